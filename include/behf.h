@@ -1,0 +1,150 @@
+/*
+ * behf.h -- C ABI of the GB300 BEHF poroelastic time stepper (libbehf.so).
+ *
+ * The reference drives its GPU through one call,
+ *     void callCUDAKernel(blockInfo*, nxt, nyt, nzt, DT, F0, sn, coord, ..., NT)   (kernel.cu:1728,
+ *     declared main.cpp:59),
+ * after main.cpp has built the medium, the coefficients and the CPML profiles on the host and
+ * copied ~99 device arrays into a blockInfo (main.cpp:1529-1743).  That call then runs the whole
+ * time loop, samples txx along one line every step and writes the output files itself.
+ *
+ * This header splits that boundary into setup, run and output calls over an opaque context.
+ * Every call returns a behf_status and never exits the process (the reference's CUDA_CHECK calls
+ * exit(), kernel.cu:42-52).  A context is single-thread affine and owns one CUDA stream; separate
+ * contexts may be driven from separate threads.  All host pointers are copied; the caller keeps
+ * ownership.  Arrays are C order [nz][ny][nx] (x fastest), as the reference's
+ * offset = ix + iy*nxt + iz*nxt*nyt (kernel.cu:162).
+ */
+#ifndef BEHF_H
+#define BEHF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int behf_status;
+#define BEHF_OK 0
+#define BEHF_ERR_INVALID (-1)   /* bad argument or size */
+#define BEHF_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define BEHF_ERR_ALLOC (-3)     /* device or host allocation failed */
+#define BEHF_ERR_STATE (-4)     /* call out of order (e.g. run before the medium is set) */
+#define BEHF_ERR_NONFINITE (-5) /* the health check found a NaN/Inf or an overflow in a field */
+#define BEHF_ERR_UNSUPPORTED (-6)
+
+/* Storage precision of the wavefields (arithmetic is FP32 for the 16/32-bit kinds, FP64 for FP64). */
+typedef enum { BEHF_FP64 = 0, BEHF_FP32 = 1, BEHF_FP16 = 2, BEHF_BF16 = 3 } behf_precision;
+
+/* Field indices: solid velocity, Darcy flux, the six stresses, pore pressure.
+ * Reference names: vux vuy vuz vwx vwy vwz txx tyy tzz txy txz tyz ss (common.h:10-12). */
+enum {
+    BEHF_VX = 0, BEHF_VY, BEHF_VZ, BEHF_QX, BEHF_QY, BEHF_QZ,
+    BEHF_SXX, BEHF_SYY, BEHF_SZZ, BEHF_SXY, BEHF_SXZ, BEHF_SYZ, BEHF_P, BEHF_NFIELD
+};
+
+/* Cell-centred moduli, the outputs of the reference's create_model_all (outputfunc.cpp:153-222):
+ * rho, rho_f, mu, M, C (= alpha M), H (= lambda_u + 2 mu), lambda_u (H2u), b = eta/kappa (C1),
+ * m = (1 + 2/8) tau rho_f / phi (C2). */
+enum { BEHF_RHO = 0, BEHF_RHOF, BEHF_MU, BEHF_M, BEHF_C, BEHF_HH, BEHF_H2U, BEHF_C1, BEHF_C2, BEHF_NMOD };
+
+/* Source kinds.  EXPLOSIVE adds the wavelet to txx, tyy, tzz before the velocity update, as the
+ * reference's Source kernel does (kernel.cu:130-142).  PRESSURE adds it to the pore pressure.
+ * FORCE_Z adds wavelet * dt / rho_z to vz after the velocity update (a body-force density). */
+typedef enum { BEHF_SRC_EXPLOSIVE = 0, BEHF_SRC_PRESSURE = 1, BEHF_SRC_FORCE_Z = 2 } behf_source_kind;
+
+typedef struct {
+    int nx, ny, nz;          /* grid incl. CPML cells and the never-updated ghost ring of width radius */
+    double h;                /* grid spacing (m); the reference hard-codes 1/h = 100 (kernel.cu:158) */
+    double dt;               /* time step (s) */
+    int radius;              /* staggered stencil half-width R, 1..4 (order 2R; the reference is R = 1) */
+    int cpml_width;          /* CPML cells per face L (reference NP, main.cpp:23); 0 = none */
+    double cpml_v0;          /* profile velocity (reference v0 = 4000, main.cpp:558) */
+    double cpml_r;           /* target reflection (reference RC = 1e-6, main.cpp:88) */
+    double scales[4];        /* per-field storage scales s_v, s_q, s_sigma, s_p; all 0 = automatic */
+    double src_amp_hint;     /* automatic scales: expected wavelet peak (0 = 1) */
+    double src_f0_hint;      /* automatic scales: dominant frequency in Hz (0 = 30) */
+} behf_grid;
+
+typedef struct behf_ctx behf_ctx;
+
+typedef struct {
+    int64_t step;            /* steps taken since the last reset */
+    int64_t device_bytes;    /* bytes this context holds on the device */
+    double scales[4];        /* scales in use */
+    double bytes_per_cell;   /* algorithmic HBM bytes of one cell update (state + coefficients + CPML) */
+    int kernel;              /* kernel family in use (behf_kernel) */
+    int radius, precision;
+} behf_info;
+
+/* Kernel family: PLAIN = one thread per cell with cached neighbour loads; TILED = the z-marching
+ * shared-memory kernel (FP16/BF16/FP32, R = 4 and R = 1).  AUTO picks TILED where it exists. */
+typedef enum { BEHF_KERNEL_AUTO = 0, BEHF_KERNEL_PLAIN = 1, BEHF_KERNEL_TILED = 2 } behf_kernel;
+
+/* Options for behf_set_option. */
+enum {
+    BEHF_OPT_KERNEL = 0,         /* behf_kernel */
+    BEHF_OPT_REF_BUG_COMPAT = 1, /* 1: vz Darcy update uses the y-staggered VW3 as kernel.cu:220 does */
+    BEHF_OPT_GRAPH_CHUNK = 2,    /* steps per captured CUDA graph (0 = no graph) */
+};
+
+/* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current
+ * device.  Replaces main.cpp:1529-1627 (cudaMalloc of the blockInfo arrays). */
+behf_status behf_create(const behf_grid* grid, int precision, behf_ctx** out);
+behf_status behf_destroy(behf_ctx* ctx);
+
+/* Medium from host arrays (copied), moduli[BEHF_NMOD] each [nz][ny][nx] float.  Builds the staggered
+ * coefficients on the device.  Replaces main.cpp:322-494 (averaging + coefficients), 1482-1526
+ * (FP16 conversion) and 1640-1743 (H2D copies). */
+behf_status behf_set_medium(behf_ctx* ctx, const float* const moduli[BEHF_NMOD]);
+/* Same, from device arrays (not freed, not kept). */
+behf_status behf_set_medium_device(behf_ctx* ctx, const float* const moduli[BEHF_NMOD]);
+
+/* Explicit 1-D CPML profiles for one axis (0 = x, 1 = y, 2 = z), n entries each: damping d at the
+ * integer points and d2 at the half-shifted points (1/s).  Overrides the profile built from
+ * cpml_width/v0/r (main.cpp:519-1371).  Call before behf_set_medium or behf_reset. */
+behf_status behf_set_cpml_profile(behf_ctx* ctx, int axis, const double* d, const double* d2);
+
+/* Source at cell (ix, iy, iz) with wavelet[nt] (host, copied).  Steps past nt inject nothing.
+ * Replaces the Ricker/Source pair of kernel.cu:1898,2064-2071 (host value + full-grid launch). */
+behf_status behf_set_source(behf_ctx* ctx, int kind, int ix, int iy, int iz, const float* wavelet, int nt);
+
+/* Receivers: ijk[3*nrec] cell indices (ix, iy, iz), comp[nrec] field indices.  Sampled on the
+ * device after every step into an FP64 [nrec][capacity] buffer; replaces the per-step full-volume
+ * D2H copy and host pick of kernel.cu:2197-2243. */
+behf_status behf_set_receivers(behf_ctx* ctx, int nrec, const int* ijk, const int* comp, int capacity);
+
+/* Advance nsteps time steps (Source -> V -> T -> receivers each step, kernel.cu:2064-2192 order).
+ * behf_run waits for completion; behf_run_async only enqueues on the context's stream. */
+behf_status behf_run(behf_ctx* ctx, int nsteps);
+behf_status behf_run_async(behf_ctx* ctx, int nsteps);
+behf_status behf_sync(behf_ctx* ctx);
+
+/* Seismograms recorded so far, physical units, [nrec][nsteps_recorded] into out (host). */
+behf_status behf_get_seismograms(behf_ctx* ctx, double* out, int* nsteps_recorded);
+/* One field in physical units, [nz][ny][nx] float (host).  For wfile3d-style snapshots. */
+behf_status behf_get_field(behf_ctx* ctx, int field, float* out);
+behf_status behf_set_field(behf_ctx* ctx, int field, const float* in);
+/* Zero wavefields, CPML memory and seismograms; step = 0.  Keeps medium, source and receivers. */
+behf_status behf_reset(behf_ctx* ctx);
+
+behf_status behf_set_option(behf_ctx* ctx, int option, int value);
+behf_status behf_get_info(behf_ctx* ctx, behf_info* out);
+/* The context's cudaStream_t, for event timing by the caller. */
+behf_status behf_get_stream(behf_ctx* ctx, void** stream);
+
+/* Health check (energy-norm reduction in FP64 over every field, on the device): writes the sum of
+ * squares of each field in storage units to norms[BEHF_NFIELD] and returns BEHF_ERR_NONFINITE if any
+ * value is NaN/Inf or saturates the storage format.  The reference has no counterpart (it prints
+ * or ignores errors, kernel.cu:1926-1929). */
+behf_status behf_health(behf_ctx* ctx, double* norms);
+
+/* Text of the last error on this thread. */
+const char* behf_last_error(void);
+/* Library version string. */
+const char* behf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

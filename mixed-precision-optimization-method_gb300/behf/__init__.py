@@ -1,0 +1,242 @@
+"""Python front end of libbehf (GB300 BEHF poroelastic time stepper), over its C ABI via ctypes.
+
+The compute path is the CUDA library ``behf/_lib/libbehf.so`` (built by ``behf.build``); this module
+only moves host arrays across the C ABI declared in ``include/behf.h``.  There is no CPU fallback:
+if the library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libbehf.so"
+_lib = None
+
+FIELDS = ["vx", "vy", "vz", "qx", "qy", "qz", "sxx", "syy", "szz", "sxy", "sxz", "syz", "p"]
+FIELD = {n: i for i, n in enumerate(FIELDS)}
+MODULI = ["rho", "rhof", "mu", "M", "C", "HH", "H2u", "C1", "C2"]
+PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
+SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
+KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
+OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK = 0, 1, 2
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
+          -5: "non-finite or saturated field", -6: "unsupported"}
+
+
+class BehfError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("dt", C.c_double),
+                ("radius", C.c_int), ("cpml_width", C.c_int), ("cpml_v0", C.c_double), ("cpml_r", C.c_double),
+                ("scales", C.c_double * 4), ("src_amp_hint", C.c_double), ("src_f0_hint", C.c_double)]
+
+
+class Info(C.Structure):
+    _fields_ = [("step", C.c_int64), ("device_bytes", C.c_int64), ("scales", C.c_double * 4),
+                ("bytes_per_cell", C.c_double), ("kernel", C.c_int), ("radius", C.c_int), ("precision", C.c_int)]
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load() -> C.CDLL:
+    """Load libbehf.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        raise RuntimeError(f"{_LIB_PATH} is missing: build it with behf.build.build()")
+    lib = C.CDLL(str(_LIB_PATH))
+    P = C.POINTER
+    sig = {
+        "behf_create": [P(Grid), C.c_int, P(C.c_void_p)],
+        "behf_destroy": [C.c_void_p],
+        "behf_set_medium": [C.c_void_p, P(P(C.c_float))],
+        "behf_set_medium_device": [C.c_void_p, P(C.c_void_p)],
+        "behf_set_cpml_profile": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double)],
+        "behf_set_source": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_float), C.c_int],
+        "behf_set_receivers": [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), C.c_int],
+        "behf_run": [C.c_void_p, C.c_int],
+        "behf_run_async": [C.c_void_p, C.c_int],
+        "behf_sync": [C.c_void_p],
+        "behf_get_seismograms": [C.c_void_p, P(C.c_double), P(C.c_int)],
+        "behf_get_field": [C.c_void_p, C.c_int, P(C.c_float)],
+        "behf_set_field": [C.c_void_p, C.c_int, P(C.c_float)],
+        "behf_reset": [C.c_void_p],
+        "behf_set_option": [C.c_void_p, C.c_int, C.c_int],
+        "behf_get_info": [C.c_void_p, P(Info)],
+        "behf_get_stream": [C.c_void_p, P(C.c_void_p)],
+        "behf_health": [C.c_void_p, P(C.c_double)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.behf_last_error.restype = C.c_char_p
+    lib.behf_last_error.argtypes = []
+    lib.behf_version.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(code: int):
+    if code != 0:
+        raise BehfError(code, load().behf_last_error().decode())
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Solver:
+    """One BEHF context on the current CUDA device (owns its stream and device memory)."""
+
+    def __init__(self, nx, ny, nz, h, dt, radius=4, precision="f16", cpml_width=10, cpml_v0=4000.0,
+                 cpml_r=1e-6, scales=None, src_amp_hint=0.0, src_f0_hint=0.0):
+        self._lib = load()
+        g = Grid()
+        g.nx, g.ny, g.nz, g.h, g.dt, g.radius = nx, ny, nz, h, dt, radius
+        g.cpml_width, g.cpml_v0, g.cpml_r = cpml_width, cpml_v0, cpml_r
+        for i in range(4):
+            g.scales[i] = 0.0 if scales is None else float(scales[i])
+        g.src_amp_hint, g.src_f0_hint = src_amp_hint, src_f0_hint
+        self.grid = g
+        self.shape = (nz, ny, nx)
+        self.precision = precision
+        self._ctx = C.c_void_p()
+        _check(self._lib.behf_create(C.byref(g), PRECISION[precision], C.byref(self._ctx)))
+        self.nrec = 0
+
+    # -- lifecycle
+    def close(self):
+        if self._ctx:
+            self._lib.behf_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- set-up
+    def set_medium(self, mod: np.ndarray):
+        mod = _f32(mod)
+        assert mod.shape == (9, *self.shape), mod.shape
+        ptrs = (C.POINTER(C.c_float) * 9)(*[mod[i].ctypes.data_as(C.POINTER(C.c_float)) for i in range(9)])
+        _check(self._lib.behf_set_medium(self._ctx, ptrs))
+
+    def set_medium_device(self, ptrs: list[int]):
+        arr = (C.c_void_p * 9)(*ptrs)
+        _check(self._lib.behf_set_medium_device(self._ctx, arr))
+
+    def set_cpml_profile(self, axis: int, d: np.ndarray, d2: np.ndarray):
+        d = np.ascontiguousarray(d, np.float64)
+        d2 = np.ascontiguousarray(d2, np.float64)
+        _check(self._lib.behf_set_cpml_profile(self._ctx, axis, d.ctypes.data_as(C.POINTER(C.c_double)),
+                                               d2.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def set_source(self, kind: str, ijk, wavelet: np.ndarray):
+        w = _f32(wavelet)
+        _check(self._lib.behf_set_source(self._ctx, SOURCE[kind], int(ijk[0]), int(ijk[1]), int(ijk[2]),
+                                         w.ctypes.data_as(C.POINTER(C.c_float)), int(w.shape[0])))
+
+    def set_receivers(self, ijk: np.ndarray, comp: np.ndarray, capacity: int):
+        ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        comp = np.ascontiguousarray(comp, np.int32)
+        self.nrec = comp.shape[0]
+        _check(self._lib.behf_set_receivers(self._ctx, self.nrec, ijk.ctypes.data_as(C.POINTER(C.c_int)),
+                                            comp.ctypes.data_as(C.POINTER(C.c_int)), int(capacity)))
+
+    def set_option(self, opt: int, value: int):
+        _check(self._lib.behf_set_option(self._ctx, opt, int(value)))
+
+    def set_kernel(self, name: str):
+        self.set_option(OPT_KERNEL, KERNEL[name])
+
+    # -- running
+    def run(self, nsteps: int):
+        _check(self._lib.behf_run(self._ctx, int(nsteps)))
+
+    def run_async(self, nsteps: int):
+        _check(self._lib.behf_run_async(self._ctx, int(nsteps)))
+
+    def sync(self):
+        _check(self._lib.behf_sync(self._ctx))
+
+    def reset(self):
+        _check(self._lib.behf_reset(self._ctx))
+
+    # -- outputs
+    def seismograms(self) -> np.ndarray:
+        ns = C.c_int(0)
+        _check(self._lib.behf_get_seismograms(self._ctx, None, C.byref(ns)))
+        out = np.zeros((self.nrec, ns.value), np.float64)
+        if self.nrec and ns.value:
+            _check(self._lib.behf_get_seismograms(self._ctx, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  C.byref(ns)))
+        return out
+
+    def get_field(self, name) -> np.ndarray:
+        q = FIELD[name] if isinstance(name, str) else int(name)
+        out = np.zeros(self.shape, np.float32)
+        _check(self._lib.behf_get_field(self._ctx, q, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_field(self, name, values: np.ndarray):
+        q = FIELD[name] if isinstance(name, str) else int(name)
+        v = _f32(values)
+        assert v.shape == self.shape
+        _check(self._lib.behf_set_field(self._ctx, q, v.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def info(self) -> dict:
+        inf = Info()
+        _check(self._lib.behf_get_info(self._ctx, C.byref(inf)))
+        return {"step": inf.step, "device_bytes": inf.device_bytes, "scales": tuple(inf.scales),
+                "bytes_per_cell": inf.bytes_per_cell, "kernel": {0: "auto", 1: "plain", 2: "tiled"}[inf.kernel],
+                "radius": inf.radius, "precision": inf.precision}
+
+    def health(self):
+        norms = np.zeros(13, np.float64)
+        code = self._lib.behf_health(self._ctx, norms.ctypes.data_as(C.POINTER(C.c_double)))
+        if code not in (0, -5):
+            _check(code)
+        return code == 0, norms
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self._lib.behf_get_stream(self._ctx, C.byref(s)))
+        return s.value or 0
+
+
+def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None) -> Solver:
+    """A Solver set up with a problem description (see behf.problems.Problem)."""
+    s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
+               cpml_width=prob.cpml_width, cpml_v0=prob.cpml_v0, cpml_r=prob.cpml_r, scales=scales,
+               src_amp_hint=float(np.abs(prob.wavelet).max()) if prob.wavelet.size else 1.0,
+               src_f0_hint=prob.f0)
+    if prob.ref_bug_compat:
+        s.set_option(OPT_REF_BUG_COMPAT, 1)
+    s.set_kernel(kernel)
+    s.set_medium(prob.mod)
+    s.set_source(prob.src_kind, prob.src, prob.wavelet)
+    if len(prob.rec_comp):
+        s.set_receivers(prob.rec_ijk, prob.rec_comp, prob.nt if capacity is None else capacity)
+    return s
+
+
+__all__ = ["Solver", "BehfError", "solver_for", "load", "lib_path", "FIELDS", "FIELD", "MODULI"]

@@ -1,0 +1,253 @@
+"""Problem descriptions: media, sources, receivers and the named workloads.
+
+A ``Problem`` carries everything one forward run needs (grid, cell-centred moduli, wavelet, source,
+receivers, CPML) so that the same description drives the CUDA library and the CPU oracle.
+
+Media restate the reference's Biot-Gassmann relations (outputfunc.cpp:202-217):
+    rho = (1-phi) rho_s + phi rho_f,  alpha = 1 - K_dry/K_s,
+    M = K_f K_s / (phi K_s + (alpha - phi) K_f),  H = alpha^2 M + K_dry + 4 mu / 3,
+    lambda_u = H - 2 mu,  C = alpha M,  b = eta / kappa,  m = (1 + 2/8) tau rho_f / phi
+(the shape factor 8 is the reference's ``porousm``, outputfunc.cpp:164).  A cell with phi = 1 is pure
+fluid, as the reference's borehole cells (outputfunc.cpp:169-187).
+
+Named workloads (sizes, steps and media of the benchmark and parity cases):
+    small64       64^3, h = 5 m, dt = 0.4 ms, 500 steps, 10-cell CPML, homogeneous sandstone,
+                  explosive source at the centre, 30 Hz Ricker, 32 receivers on a line (vz and p)
+    layered256    256^3, 2000 steps, 20-cell CPML, sandstone over a stiffer layer at z = 640 m,
+                  25 Hz explosive source, 16 x 16 surface receivers (vz and p)
+    random1024    1024^3, 3000 steps, 20-cell CPML, sandstone with 5 % Gaussian-correlated (50 m)
+                  perturbations of K_dry, mu, phi and log-normal kappa (sigma 0.5), vertical force
+                  source, 20 Hz, 512 x 512 surface receivers (vz and p)
+    borehole      the reference's own problem: 240 x 240 x 360 cells of 1 cm (180^2 x 300 + 30-cell
+                  CPML), fluid borehole in a porous formation, 10 kHz, 3500 steps of 1 us, radius 1,
+                  txx recorded on the vertical line through the source (main.cpp:20-23, 84-99)
+Each accepts a ``scale`` (grid shrink factor) and ``nt`` override for test-sized variants.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SANDSTONE = dict(Ks=37e9, Kf=2.25e9, Kdry=9e9, mu=7e9, rhos=2650.0, rhof=1000.0, phi=0.2, kappa=1e-12,
+                 eta=1e-3, tau=2.4)
+STIFF = dict(SANDSTONE, Kdry=20e9, mu=15e9, phi=0.1, kappa=1e-14)
+
+
+def rock_moduli(Ks, Kf, Kdry, mu, rhos, rhof, phi, kappa, eta, tau):
+    """Cell-centred moduli [9, ...] (rho, rhof, mu, M, C, HH, H2u, C1, C2) from rock parameters (arrays ok)."""
+    Ks, Kf, Kdry, mu, rhos, rhof, phi, kappa, eta, tau = np.broadcast_arrays(
+        *[np.asarray(v, np.float64) for v in (Ks, Kf, Kdry, mu, rhos, rhof, phi, kappa, eta, tau)])
+    porousm = 8.0
+    rho = (1 - phi) * rhos + phi * rhof
+    a = 1 - Kdry / Ks
+    M = Kf * Ks / (phi * Ks + (a - phi) * Kf)
+    HH = a * a * M + Kdry + mu * 4.0 / 3.0
+    out = np.stack([rho, rhof, mu, M, M * a, HH, HH - 2 * mu, eta / kappa, (1 + 2 / porousm) * tau * rhof / phi])
+    fluid = phi >= 1.0
+    if np.any(fluid):
+        out[0][fluid] = rhof[fluid]
+        out[2][fluid] = 0.0
+        for q in (3, 4, 5, 6):
+            out[q][fluid] = Kf[fluid]
+        out[7][fluid] = 0.0
+        out[8][fluid] = rhof[fluid]
+    return out
+
+
+def p_velocity(rock: dict) -> float:
+    m = rock_moduli(**rock)
+    return float(np.sqrt(m[5] / m[0]))
+
+
+def gaussian_random_field(shape, corr_cells: float, seed: int) -> np.ndarray:
+    """Zero-mean, unit-variance field with correlation exp(-r^2 / l^2), l = corr_cells (float64).
+
+    White noise smoothed by a separable Gaussian of std l/2 (periodic wrap), normalised by the
+    filter's analytic gain sqrt(sum g^2)^3."""
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal(shape)
+    sig = corr_cells / 2.0
+    half = int(np.ceil(4 * sig))
+    x = np.arange(-half, half + 1)
+    g = np.exp(-0.5 * (x / sig) ** 2)
+    g /= g.sum()
+    for ax in range(3):
+        acc = np.zeros_like(f)
+        for k, w in zip(x, g):
+            acc += w * np.roll(f, k, axis=ax)
+        f = acc
+    return f / np.sqrt(np.sum(g * g)) ** 3
+
+
+@dataclass
+class Problem:
+    nx: int
+    ny: int
+    nz: int
+    h: float
+    dt: float
+    radius: int
+    mod: np.ndarray                  # float32 [9, nz, ny, nx]
+    wavelet: np.ndarray              # float32 [nt]
+    src: tuple
+    rec_ijk: np.ndarray              # int32 [nrec, 3]  (ix, iy, iz)
+    rec_comp: np.ndarray             # int32 [nrec]
+    src_kind: str = "explosive"
+    cpml_width: int = 10
+    cpml_v0: float = 4000.0
+    cpml_r: float = 1e-6
+    f0: float = 30.0
+    ref_bug_compat: bool = False
+    scales: tuple = (1.0, 1.0, 1.0, 1.0)
+    name: str = ""
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nt(self) -> int:
+        return int(self.wavelet.shape[0])
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def auto_scales(mod: np.ndarray, amp: float = 1.0, f0: float = 30.0) -> tuple:
+    """The library's automatic storage scales (powers of two), from the moduli and the wavelet:
+    s_sigma = s_p = 1/amp, s_v = s_sigma * max sqrt(rho H) (fast-P impedance), and
+    s_q = s_v * clamp(b_min / (rho_max 2 pi f0), 1, 1e6) so the Darcy flux, which is smaller than v by
+    about rho omega / b at low frequency, lands in the same range."""
+    rho = np.maximum(mod[0].astype(np.float64), 0)
+    hh = np.maximum(mod[5].astype(np.float64), 0)
+    c1 = mod[7].astype(np.float64)
+    zmax = float(np.sqrt(rho * hh).max())
+    rmax = float(rho.max())
+    pos = c1[c1 > 0]
+    ss = 1.0 / amp
+    sv = ss * (zmax if zmax > 0 else 1.0)
+    kq = float(pos.min()) / (rmax * 2 * np.pi * f0) if pos.size and rmax > 0 else 1.0
+    kq = min(max(kq, 1.0), 1e6)
+    p2 = lambda v: float(2.0 ** round(np.log2(v)))
+    return (p2(sv), p2(sv * kq), p2(ss), p2(ss))
+
+
+def ricker(nt: int, dt: float, f0: float, t0: float | None = None, amp: float = 1.0) -> np.ndarray:
+    """Ricker wavelet of kernel.cu:1898: amp * -(1 - 2 pi^2 f^2 tau^2) exp(-pi^2 f^2 tau^2), tau = t - t0,
+    t0 = 1.2/f by default (kernel.cu:1730)."""
+    t0 = 1.2 / f0 if t0 is None else t0
+    tau = np.arange(nt) * dt - t0
+    a = (np.pi * f0 * tau) ** 2
+    return (amp * -(1 - 2 * a) * np.exp(-a)).astype(np.float32)
+
+
+def homogeneous(shape, rock=SANDSTONE) -> np.ndarray:
+    m = rock_moduli(**rock)
+    return np.broadcast_to(m[:, None, None, None], (9, *shape)).astype(np.float32)
+
+
+def layered(shape, rocks, interfaces) -> np.ndarray:
+    """Layers in z: rocks[0] above interfaces[0] (cell index), rocks[1] below, ..."""
+    nz = shape[0]
+    out = np.empty((9, *shape), np.float32)
+    bounds = [0, *interfaces, nz]
+    for r, (z0, z1) in zip(rocks, zip(bounds[:-1], bounds[1:])):
+        out[:, z0:z1] = rock_moduli(**r)[:, None, None, None]
+    return out
+
+
+def random_medium(shape, rock=SANDSTONE, seed=1234, corr_cells=10.0, pct=0.05, log_kappa_sigma=0.5):
+    g = [gaussian_random_field(shape, corr_cells, seed + i) for i in range(4)]
+    p = dict(rock)
+    p["Kdry"] = rock["Kdry"] * (1 + pct * g[0])
+    p["mu"] = rock["mu"] * (1 + pct * g[1])
+    p["phi"] = rock["phi"] * (1 + pct * g[2])
+    p["kappa"] = rock["kappa"] * np.exp(log_kappa_sigma * g[3])
+    return rock_moduli(**p).astype(np.float32)
+
+
+def line_receivers(ix, iy, iz, comps):
+    ix, iy, iz = np.broadcast_arrays(np.atleast_1d(ix), np.atleast_1d(iy), np.atleast_1d(iz))
+    ijk = np.stack([ix, iy, iz], 1).astype(np.int32)
+    ijk = np.repeat(ijk, len(comps), axis=0)
+    comp = np.tile(np.asarray(comps, np.int32), len(ix))
+    return ijk, comp
+
+
+def small64(n=64, nt=500, radius=4, cpml=10) -> Problem:
+    h, dt, f0 = 5.0, 4e-4, 30.0
+    shape = (n, n, n)
+    c = n // 2
+    xs = np.linspace(cpml + 2, n - cpml - 3, 32).round().astype(int)
+    ijk, comp = line_receivers(xs, c, min(c + 10, n - cpml - 2), [2, 12])
+    return Problem(n, n, n, h, dt, radius, homogeneous(shape), ricker(nt, dt, f0), (c, c, c), ijk, comp,
+                   cpml_width=cpml, cpml_v0=p_velocity(SANDSTONE), f0=f0, name=f"small{n}")
+
+
+def layered256(n=256, nt=2000, radius=4, cpml=20, nrec_side=16) -> Problem:
+    h, dt, f0 = 5.0, 4e-4, 25.0
+    shape = (n, n, n)
+    zi = n // 2  # z = 640 m at 256 cells of 5 m
+    mod = layered(shape, [SANDSTONE, STIFF], [zi])
+    c = n // 2
+    ax = np.linspace(cpml + 4, n - cpml - 5, nrec_side).round().astype(int)
+    X, Y = np.meshgrid(ax, ax, indexing="xy")
+    ijk, comp = line_receivers(X.ravel(), Y.ravel(), cpml + 2, [2, 12])
+    src = (c, c, max(cpml + 6, (cpml + zi) // 2))
+    return Problem(n, n, n, h, dt, radius, mod, ricker(nt, dt, f0), src, ijk, comp, cpml_width=cpml,
+                   cpml_v0=p_velocity(STIFF), f0=f0, name=f"layered{n}")
+
+
+def random1024(n=1024, nt=3000, radius=4, cpml=20, nrec_side=512, seed=1234, medium=True) -> Problem:
+    """The 1024^3 random medium; with medium=False the moduli are left for the device generator."""
+    h, dt, f0 = 5.0, 4e-4, 20.0
+    shape = (n, n, n)
+    mod = random_medium(shape, seed=seed) if medium else np.zeros((9, 1, 1, 1), np.float32)
+    c = n // 2
+    ax = np.linspace(cpml + 2, n - cpml - 3, nrec_side).round().astype(int)
+    X, Y = np.meshgrid(ax, ax, indexing="xy")
+    ijk, comp = line_receivers(X.ravel(), Y.ravel(), cpml + 2, [2, 12])
+    src = (c, c, min(n // 4, n - cpml - 6))
+    return Problem(n, n, n, h, dt, radius, mod, ricker(nt, dt, f0), src, ijk, comp, src_kind="force_z",
+                   cpml_width=cpml, cpml_v0=p_velocity(SANDSTONE) * 1.1, f0=f0, name=f"random{n}",
+                   extra={"seed": seed})
+
+
+def borehole_moduli(nz, ny, nx) -> np.ndarray:
+    """The reference's borehole medium (outputfunc.cpp:153-222) with its float/double rounding."""
+    out = np.zeros((9, nz, ny, nx), np.float32)
+    iy, ix = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    fluid = ((ix - nx // 2) ** 2 + (iy - ny // 2) ** 2) <= 100
+    f32 = np.float32
+    # formation (float volumes, double rock constants, HH from the float-rounded M)
+    vp, vs, rhos, rhof, vf, por = f32(5000), f32(3300), f32(2450), f32(1000), f32(1500), 0.1
+    rho = f32((1 - por) * rhos + por * rhof)
+    mu = f32((1 - por) * float(rhos) * float(vs) * float(vs))
+    kb = float(rhos) * (1 - por) * (float(f32(vp * vp)) - float(f32(vs * vs)) * 4.0 / 3.0)
+    ks = float(rhos) * (float(f32(vp * vp)) - float(f32(vs * vs)) * 4.0 / 3.0)
+    kf = float(f32(f32(rhof * vf) * vf))
+    a1 = 1 - kb / ks
+    M = f32(kf * ks / (por * ks + (a1 - por) * kf))
+    HH = f32(a1 * a1 * float(M) + kb + float(mu) * 4.0 / 3.0)
+    form = [rho, rhof, mu, M, f32(float(M) * a1), HH, f32(HH - f32(2) * mu), f32(1e-3 / (2e-12)),
+            f32((1 + 2 / 8.0) * 3.0 * float(rhof) / por)]
+    kff = f32(f32(f32(1000) * f32(1500)) * f32(1500))
+    flu = [f32(1000), f32(1000), f32(0), kff, kff, kff, kff, f32(0), f32(1000)]
+    for q in range(9):
+        out[q] = np.where(fluid, flu[q], form[q])[None]
+    return out
+
+
+def borehole(scale: float = 1.0, nt=3500) -> Problem:
+    """The reference's problem (main.cpp:20-23, 84-99), optionally shrunk by ``scale`` (cells)."""
+    NX, NY, NZ, NP = (max(24, int(round(v * scale))) for v in (180, 180, 300, 30))
+    NP = max(4, int(round(30 * scale)))
+    nx, ny, nz = NX + 2 * NP, NY + 2 * NP, NZ + 2 * NP
+    h, dt, f0 = 0.01, 1e-6, 1e4
+    sx, sy, sz = nx // 2, ny // 2, min(20 + NP, nz - NP - 2)
+    ijk, comp = line_receivers(sx, sy, np.arange(1, nz - 1), [6])
+    return Problem(nx, ny, nz, h, dt, 1, borehole_moduli(nz, ny, nx), ricker(nt, dt, f0), (sx, sy, sz), ijk, comp,
+                   cpml_width=NP, cpml_v0=4000.0, cpml_r=1e-6, f0=f0, ref_bug_compat=True,
+                   scales=(1e8, 1e8, 1.0, 1.0), name="borehole")
+
+
+WORKLOADS = {"small64": small64, "layered256": layered256, "random1024": random1024, "borehole": borehole}

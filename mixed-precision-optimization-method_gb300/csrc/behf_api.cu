@@ -1,0 +1,771 @@
+// behf_api.cu -- the C ABI of libbehf (include/behf.h): context, device memory, set-up and the
+// graph-captured time loop.  Replaces the reference's host/device boundary: main.cpp:1529-1743
+// (allocation and copies of the blockInfo arrays) and callCUDAKernel (kernel.cu:1728-2698).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "behf_aux.cuh"
+#include "behf_internal.cuh"
+
+using namespace behf;
+
+namespace {
+thread_local std::string g_err;
+
+behf_status fail(behf_status code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(BEHF_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                 \
+    } while (0)
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t elem_size(int prec) { return prec == BEHF_FP64 ? 8 : prec == BEHF_FP32 ? 4 : 2; }
+size_t kelem_size(int prec) { return prec == BEHF_FP64 ? 8 : prec == BEHF_FP32 ? 4 : 2; }
+size_t welem_size(int prec) { return prec == BEHF_FP64 ? 8 : 4; }  // CPML memory, VW1, profiles
+
+// CPML profile of one axis (main.cpp:537-563): quadratic d on the slabs [0,L) and [n-1-L, n),
+// half-shifted d2, d0 = 3 v0 ln(1/R) / (2 L h).
+void cpml_profile(int n, int L, double h, double v0, double rc, std::vector<double>& d, std::vector<double>& d2) {
+    d.assign(n, 0.0);
+    d2.assign(n, 0.0);
+    if (L <= 0) return;
+    const double DP = L * h, d0 = 3.0 * v0 * std::log(1.0 / rc) / (2.0 * DP);
+    const double xl = DP, xr = (n - 1) * h - DP;
+    for (int i = 0; i < n; i++) {
+        const double x = i * h;
+        if (i < L) {
+            d[i] = d0 * std::pow((xl - x) / DP, 2);
+            d2[i] = d0 * std::pow((xl - x - 0.5 * h) / DP, 2);
+        } else if (i >= n - 1 - L) {
+            d[i] = d0 * std::pow((x - xr) / DP, 2);
+            d2[i] = d0 * std::pow((x + 0.5 * h - xr) / DP, 2);
+        }
+    }
+}
+
+double pow2_round(double s) { return std::ldexp(1.0, (int)std::lround(std::log2(s))); }
+
+}  // namespace
+
+struct behf_ctx {
+    behf_grid grid{};
+    int prec = BEHF_FP32;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    Geom g{};
+    DevPtrs p{};
+    size_t es = 0, ks = 0, ws = 0;
+    long long nfield = 0;  // elements per pitched array
+    std::vector<std::pair<void*, size_t>> allocs;
+    int64_t device_bytes = 0;
+    float* d_rho = nullptr;  // cell-centred density kept for the force source
+    double scales[4] = {1, 1, 1, 1};
+    bool auto_scales = true, medium_set = false;
+    // profile overrides
+    bool prof_override[3] = {false, false, false};
+    std::vector<double> prof_d[3], prof_d2[3];
+    // source
+    bool src_set = false;
+    int src_kind = 0, src_ijk[3] = {0, 0, 0};
+    float* d_wavelet = nullptr;
+    int nw = 0;
+    // receivers
+    int nrec = 0, cap = 0;
+    long long* d_rec_off = nullptr;
+    int* d_rec_comp = nullptr;
+    double* d_seis = nullptr;
+    // time
+    int* d_it = nullptr;
+    long long step = 0;
+    // graph
+    int chunk = 16;
+    cudaGraphExec_t gexec = nullptr;
+    int kernel_opt = BEHF_KERNEL_AUTO;
+    // health scratch
+    double* d_part = nullptr;
+    int* d_flag = nullptr;
+    double* d_norm = nullptr;
+    int nblk_health = 0;
+
+    ~behf_ctx() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        for (auto& a : allocs) cudaFree(a.first);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    behf_status dalloc(void** out, size_t bytes) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaMalloc(&ptr, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(BEHF_ERR_ALLOC, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        }
+        allocs.emplace_back(ptr, bytes);
+        device_bytes += (int64_t)bytes;
+        *out = ptr;
+        return BEHF_OK;
+    }
+    void dfree(void* ptr) {
+        if (!ptr) return;
+        for (size_t i = 0; i < allocs.size(); i++)
+            if (allocs[i].first == ptr) {
+                device_bytes -= (int64_t)allocs[i].second;
+                allocs.erase(allocs.begin() + i);
+                break;
+            }
+        cudaFree(ptr);
+    }
+    void invalidate_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    long long cell_offset(int i, int j, int k) const { return (long long)k * g.plane + (long long)j * g.px + i; }
+    double field_scale(int q) const {
+        return q <= BEHF_VZ ? scales[0] : q <= BEHF_QZ ? scales[1] : q <= BEHF_SYZ ? scales[2] : scales[3];
+    }
+};
+
+namespace {
+
+template <class S>
+cudaError_t launch_update(behf_ctx* c, bool vel) {
+    const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && tiled_supported<S>(c->g);
+    if (tiled) return launch_tiled<S>(c->g, c->p, vel, c->stream);
+    return launch_plain<S>(c->g, c->p, vel, c->stream);
+}
+
+cudaError_t dispatch_update(behf_ctx* c, bool vel) {
+    switch (c->prec) {
+        case BEHF_FP64: return launch_update<double>(c, vel);
+        case BEHF_FP32: return launch_update<float>(c, vel);
+        case BEHF_FP16: return launch_update<__half>(c, vel);
+        case BEHF_BF16: return launch_update<__nv_bfloat16>(c, vel);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// Source injection factor: storage scale of the injected field, or dt / rho_z * s_v for the force
+// (rho_z = arithmetic mean along z, main.cpp:353).  Host copies: call outside graph capture.
+cudaError_t source_factor(behf_ctx* c, double* fac) {
+    *fac = 0;
+    if (!c->src_set) return cudaSuccess;
+    if (c->src_kind == BEHF_SRC_EXPLOSIVE) *fac = c->scales[2];
+    else if (c->src_kind == BEHF_SRC_PRESSURE) *fac = c->scales[3];
+    else {
+        const long long N = (long long)c->grid.nx * c->grid.ny;
+        const long long o = ((long long)c->src_ijk[2] * c->grid.ny + c->src_ijk[1]) * c->grid.nx + c->src_ijk[0];
+        float r0 = 0, r1 = 0;
+        cudaError_t e = cudaMemcpy(&r0, c->d_rho + o, 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(&r1, c->d_rho + o + N, 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+        const double rz = 0.5 * ((double)r0 + (double)r1);
+        *fac = rz > 0 ? c->grid.dt / rz * c->scales[0] : 0.0;
+    }
+    return cudaSuccess;
+}
+
+template <class S>
+cudaError_t enqueue_steps_t(behf_ctx* c, int n, double fac) {
+    const long long so = c->src_set ? c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]) : 0;
+    RecScales rs;
+    for (int q = 0; q < kNField; q++) rs.s[q] = c->field_scale(q);
+    for (int s = 0; s < n; s++) {
+        cudaError_t e;
+        if (c->src_set && c->src_kind != BEHF_SRC_FORCE_Z) {
+            e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, s, fac, c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        if ((e = dispatch_update(c, true)) != cudaSuccess) return e;
+        if (c->src_set && c->src_kind == BEHF_SRC_FORCE_Z) {
+            e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, s, fac, c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
+        if ((e = aux_record<S>(c->p, c->d_rec_off, c->d_rec_comp, c->nrec, c->d_seis, c->cap, c->d_it, s, rs,
+                               c->stream)) != cudaSuccess)
+            return e;
+    }
+    return aux_tick(c->d_it, n, c->stream);
+}
+
+cudaError_t enqueue_steps(behf_ctx* c, int n, double fac) {
+    switch (c->prec) {
+        case BEHF_FP64: return enqueue_steps_t<double>(c, n, fac);
+        case BEHF_FP32: return enqueue_steps_t<float>(c, n, fac);
+        case BEHF_FP16: return enqueue_steps_t<__half>(c, n, fac);
+        case BEHF_BF16: return enqueue_steps_t<__nv_bfloat16>(c, n, fac);
+    }
+    return cudaErrorInvalidValue;
+}
+
+behf_status upload_profiles(behf_ctx* c) {
+    const int n3[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+    const double dt = c->grid.dt;
+    for (int a = 0; a < 3; a++) {
+        std::vector<double> d, d2;
+        if (c->prof_override[a]) {
+            d = c->prof_d[a];
+            d2 = c->prof_d2[a];
+        } else {
+            cpml_profile(n3[a], c->grid.cpml_width, c->grid.h, c->grid.cpml_v0, c->grid.cpml_r, d, d2);
+        }
+        const int n = n3[a];
+        std::vector<double> A(n), B(n), A2(n), B2(n);
+        for (int i = 0; i < n; i++) {
+            // e = exp(-d dt) where the profile is active, 0 elsewhere (the reference's calloc'd e_d*)
+            const bool on = c->g.W > 0 && slab_index(i, n, c->g.L) >= 0;
+            A[i] = on ? std::exp(-d[i] * dt) : 0.0;
+            B[i] = on ? -dt * d[i] * 0.5 : 0.0;
+            A2[i] = on ? std::exp(-d2[i] * dt) : 0.0;
+            B2[i] = on ? -dt * d2[i] * 0.5 : 0.0;
+        }
+        const std::vector<double>* src[4] = {&A, &B, &A2, &B2};
+        void* dst[4] = {c->p.pa[a], c->p.pb[a], c->p.pa2[a], c->p.pb2[a]};
+        for (int t = 0; t < 4; t++) {
+            if (c->ws == 8) {
+                CK(cudaMemcpy(dst[t], src[t]->data(), n * 8, cudaMemcpyHostToDevice));
+            } else {
+                std::vector<float> f(n);
+                for (int i = 0; i < n; i++) f[i] = (float)(*src[t])[i];
+                CK(cudaMemcpy(dst[t], f.data(), n * 4, cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    return BEHF_OK;
+}
+
+behf_status zero_state(behf_ctx* c) {
+    for (int q = 0; q < kNField; q++) CK(cudaMemsetAsync(c->p.f[q], 0, c->nfield * c->es, c->stream));
+    if (c->g.W > 0) {
+        const size_t sl[3] = {(size_t)c->grid.nz * c->grid.ny * c->g.W, (size_t)c->grid.nz * c->g.W * c->grid.nx,
+                              (size_t)c->g.W * c->grid.ny * c->grid.nx};
+        for (int a = 0; a < 3; a++)
+            for (int s = 0; s < 8; s++) {
+                CK(cudaMemsetAsync(c->p.psi[a][s], 0, sl[a] * c->ws, c->stream));
+                CK(cudaMemsetAsync(c->p.prv[a][s], 0, sl[a] * c->ws, c->stream));
+            }
+    }
+    if (c->d_seis) CK(cudaMemsetAsync(c->d_seis, 0, (size_t)c->nrec * c->cap * 8, c->stream));
+    CK(cudaMemsetAsync(c->d_it, 0, sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->step = 0;
+    return BEHF_OK;
+}
+
+template <class S>
+behf_status build_coefs(behf_ctx* c, const float* const mod[kNMod]) {
+    CoefArgs a{};
+    for (int q = 0; q < kNMod; q++) a.mod[q] = mod[q];
+    a.nx = c->grid.nx;
+    a.ny = c->grid.ny;
+    a.nz = c->grid.nz;
+    a.px = c->g.px;
+    a.plane = c->g.plane;
+    a.dt = c->grid.dt;
+    const double sv = c->scales[0], sq = c->scales[1], ss = c->scales[2], sp = c->scales[3];
+    const double hi = 1.0 / c->grid.h;
+    for (int d = 0; d < 3; d++) {
+        a.ratio[VW1X + d] = 1.0;
+        a.ratio[VW2X + d] = sq / ss * hi;
+        a.ratio[VW3X + d] = sq / sp * hi;
+        a.ratio[VU1X + d] = sv / ss * hi;
+        a.ratio[VU2X + d] = sv / sq;
+    }
+    a.ratio[P1] = sp / sv * hi;
+    a.ratio[P2] = sp / sq * hi;
+    a.ratio[S1] = a.ratio[S2] = ss / sv * hi;
+    a.ratio[S3] = ss / sq * hi;
+    a.ratio[SXYC] = a.ratio[SXZC] = a.ratio[SYZC] = ss / sv * hi;
+    for (int q = 0; q < kNCoef; q++) {
+        a.inv[q] = 1.0;
+        a.out[q] = c->p.k[q];
+    }
+    unsigned long long* d_max = nullptr;
+    behf_status st = c->dalloc((void**)&d_max, kNCoef * 8);
+    if (st) return st;
+    CK(cudaMemsetAsync(d_max, 0, kNCoef * 8, c->stream));
+    a.maxbits = d_max;
+    const bool pow2 = (c->prec == BEHF_FP16 || c->prec == BEHF_BF16);
+    if (pow2) {
+        a.pass = 0;
+        CK(aux_build_coefs<S>(a, c->stream));
+        unsigned long long mb[kNCoef];
+        CK(cudaMemcpyAsync(mb, d_max, sizeof mb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (int q = 3; q < kNCoef; q++) {
+            double mx;
+            std::memcpy(&mx, &mb[q], 8);
+            int e = 0;
+            if (mx > 0) std::frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+            a.inv[q] = std::ldexp(1.0, -e);
+            c->g.kmuld[q] = std::ldexp(1.0, e);
+            c->g.kmulf[q] = (float)c->g.kmuld[q];
+        }
+    } else {
+        for (int q = 0; q < kNCoef; q++) {
+            c->g.kmuld[q] = 1.0;
+            c->g.kmulf[q] = 1.0f;
+        }
+    }
+    a.pass = 1;
+    CK(aux_build_coefs<S>(a, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->dfree(d_max);
+    return BEHF_OK;
+}
+
+behf_status set_medium_dev(behf_ctx* c, const float* const mod[kNMod]) {
+    const long long N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+    if (c->auto_scales) {
+        unsigned long long* d_st = nullptr;
+        behf_status st = c->dalloc((void**)&d_st, 3 * 8);
+        if (st) return st;
+        const double big = 1.7976931348623157e308;
+        unsigned long long init[3] = {0, 0, 0};
+        std::memcpy(&init[2], &big, 8);
+        CK(cudaMemcpyAsync(d_st, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
+        CK(aux_med_stats(mod[BEHF_RHO], mod[BEHF_HH], mod[BEHF_C1], N, d_st, c->stream));
+        unsigned long long r[3];
+        CK(cudaMemcpyAsync(r, d_st, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->dfree(d_st);
+        double zmax, rmax, bmin;
+        std::memcpy(&zmax, &r[0], 8);
+        std::memcpy(&rmax, &r[1], 8);
+        std::memcpy(&bmin, &r[2], 8);
+        const double amp = c->grid.src_amp_hint > 0 ? c->grid.src_amp_hint : 1.0;
+        const double f0 = c->grid.src_f0_hint > 0 ? c->grid.src_f0_hint : 30.0;
+        const double ss = 1.0 / amp;
+        const double sv = ss * (zmax > 0 ? zmax : 1.0);
+        double kq = (bmin < big && rmax > 0) ? bmin / (rmax * 2.0 * M_PI * f0) : 1.0;
+        kq = std::fmin(std::fmax(kq, 1.0), 1e6);
+        c->scales[0] = pow2_round(sv);
+        c->scales[1] = pow2_round(sv * kq);
+        c->scales[2] = pow2_round(ss);
+        c->scales[3] = pow2_round(ss);
+    }
+    CK(cudaMemcpyAsync(c->d_rho, mod[BEHF_RHO], N * 4, cudaMemcpyDeviceToDevice, c->stream));
+    behf_status st = BEHF_OK;
+    switch (c->prec) {
+        case BEHF_FP64: st = build_coefs<double>(c, mod); break;
+        case BEHF_FP32: st = build_coefs<float>(c, mod); break;
+        case BEHF_FP16: st = build_coefs<__half>(c, mod); break;
+        case BEHF_BF16: st = build_coefs<__nv_bfloat16>(c, mod); break;
+    }
+    if (st) return st;
+    c->medium_set = true;
+    c->invalidate_graph();
+    return BEHF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* behf_last_error(void) { return g_err.c_str(); }
+const char* behf_version(void) { return "behf-gb300 0.1 (sm_103a)"; }
+
+behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
+    if (!gr || !out) return fail(BEHF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (precision < BEHF_FP64 || precision > BEHF_BF16) return fail(BEHF_ERR_INVALID, "bad precision %d", precision);
+    const int R = gr->radius, L = gr->cpml_width;
+    if (R < 1 || R > 4) return fail(BEHF_ERR_INVALID, "radius %d not in 1..4", R);
+    if (!(gr->h > 0) || !(gr->dt > 0)) return fail(BEHF_ERR_INVALID, "h and dt must be positive");
+    const int n3[3] = {gr->nx, gr->ny, gr->nz};
+    for (int a = 0; a < 3; a++) {
+        if (n3[a] < 2 * R + 1) return fail(BEHF_ERR_INVALID, "axis %d: %d cells < 2R+1", a, n3[a]);
+        if (L < 0 || (L > 0 && n3[a] < 2 * L + 2))
+            return fail(BEHF_ERR_INVALID, "axis %d: %d cells too small for CPML width %d", a, n3[a], L);
+    }
+    if (L > 0 && (!(gr->cpml_v0 > 0) || !(gr->cpml_r > 0 && gr->cpml_r < 1)))
+        return fail(BEHF_ERR_INVALID, "CPML needs v0 > 0 and 0 < r < 1");
+    auto* c = new (std::nothrow) behf_ctx();
+    if (!c) return fail(BEHF_ERR_ALLOC, "host allocation failed");
+    c->grid = *gr;
+    c->prec = precision;
+    cudaGetDevice(&c->dev);
+    c->es = elem_size(precision);
+    c->ks = kelem_size(precision);
+    c->ws = welem_size(precision);
+    Geom& g = c->g;
+    g.nx = gr->nx;
+    g.ny = gr->ny;
+    g.nz = gr->nz;
+    g.R = R;
+    g.L = L;
+    g.W = L > 0 ? 2 * L + 1 : 0;
+    g.px = ((long long)gr->nx + 15) / 16 * 16;
+    g.plane = g.px * gr->ny;
+    g.bug = 0;
+    c->nfield = g.plane * gr->nz;
+    bool all0 = true;
+    for (int s = 0; s < 4; s++) all0 = all0 && gr->scales[s] == 0;
+    c->auto_scales = all0;
+    if (!all0) {
+        for (int s = 0; s < 4; s++) {
+            if (!(gr->scales[s] > 0)) {
+                delete c;
+                return fail(BEHF_ERR_INVALID, "scales must be all positive or all zero");
+            }
+            c->scales[s] = gr->scales[s];
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(BEHF_ERR_CUDA, "stream creation failed: %s", cudaGetErrorString(e));
+    }
+    behf_status st = BEHF_OK;
+    auto A = [&](void** ptr, size_t bytes) {
+        if (st == BEHF_OK) st = c->dalloc(ptr, align256(bytes));
+    };
+    for (int q = 0; q < kNField; q++) A(&c->p.f[q], c->nfield * c->es);
+    for (int q = 0; q < kNCoef; q++) A(&c->p.k[q], c->nfield * (q < 3 ? c->ws : c->ks));
+    if (g.W > 0) {
+        const size_t sl[3] = {(size_t)gr->nz * gr->ny * g.W, (size_t)gr->nz * g.W * gr->nx,
+                              (size_t)g.W * gr->ny * gr->nx};
+        for (int a = 0; a < 3; a++)
+            for (int s = 0; s < 8; s++) {
+                A(&c->p.psi[a][s], sl[a] * c->ws);
+                A(&c->p.prv[a][s], sl[a] * c->ws);
+            }
+    }
+    for (int a = 0; a < 3; a++) {
+        A(&c->p.pa[a], n3[a] * c->ws);
+        A(&c->p.pb[a], n3[a] * c->ws);
+        A(&c->p.pa2[a], n3[a] * c->ws);
+        A(&c->p.pb2[a], n3[a] * c->ws);
+    }
+    A((void**)&c->d_rho, (size_t)gr->nx * gr->ny * gr->nz * 4);
+    A((void**)&c->d_it, sizeof(int));
+    c->nblk_health = aux_grid_blocks();
+    A((void**)&c->d_part, (size_t)c->nblk_health * 8);
+    A((void**)&c->d_flag, sizeof(int));
+    A((void**)&c->d_norm, kNField * 8);
+    if (st) {
+        delete c;
+        return st;
+    }
+    for (int q = 0; q < kNCoef; q++) {
+        if (cudaMemsetAsync(c->p.k[q], 0, c->nfield * (q < 3 ? c->ws : c->ks), c->stream) != cudaSuccess) st = BEHF_ERR_CUDA;
+        g.kmuld[q] = 1.0;
+        g.kmulf[q] = 1.0f;
+    }
+    if (st == BEHF_OK) st = upload_profiles(c);
+    if (st == BEHF_OK) st = zero_state(c);
+    if (st) {
+        delete c;
+        return st == BEHF_ERR_CUDA && g_err.empty() ? fail(st, "initialisation failed") : st;
+    }
+    *out = c;
+    return BEHF_OK;
+}
+
+behf_status behf_destroy(behf_ctx* c) {
+    if (!c) return BEHF_OK;
+    cudaStreamSynchronize(c->stream);
+    delete c;
+    return BEHF_OK;
+}
+
+behf_status behf_set_medium_device(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
+    if (!c || !mod) return fail(BEHF_ERR_INVALID, "null argument");
+    for (int q = 0; q < kNMod; q++)
+        if (!mod[q]) return fail(BEHF_ERR_INVALID, "modulus array %d is null", q);
+    return set_medium_dev(c, mod);
+}
+
+behf_status behf_set_medium(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
+    if (!c || !mod) return fail(BEHF_ERR_INVALID, "null argument");
+    const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
+    float* dm[kNMod] = {};
+    behf_status st = BEHF_OK;
+    for (int q = 0; q < kNMod && st == BEHF_OK; q++) {
+        if (!mod[q]) st = fail(BEHF_ERR_INVALID, "modulus array %d is null", q);
+        else st = c->dalloc((void**)&dm[q], N * 4);
+        if (st == BEHF_OK) {
+            cudaError_t e = cudaMemcpyAsync(dm[q], mod[q], N * 4, cudaMemcpyHostToDevice, c->stream);
+            if (e != cudaSuccess) st = fail(BEHF_ERR_CUDA, "medium upload: %s", cudaGetErrorString(e));
+        }
+    }
+    if (st == BEHF_OK) st = set_medium_dev(c, dm);
+    cudaStreamSynchronize(c->stream);
+    for (int q = 0; q < kNMod; q++)
+        if (dm[q]) c->dfree(dm[q]);
+    return st;
+}
+
+behf_status behf_set_cpml_profile(behf_ctx* c, int axis, const double* d, const double* d2) {
+    if (!c || axis < 0 || axis > 2 || !d || !d2) return fail(BEHF_ERR_INVALID, "bad argument");
+    const int n = axis == 0 ? c->grid.nx : axis == 1 ? c->grid.ny : c->grid.nz;
+    c->prof_d[axis].assign(d, d + n);
+    c->prof_d2[axis].assign(d2, d2 + n);
+    c->prof_override[axis] = true;
+    return upload_profiles(c);
+}
+
+behf_status behf_set_source(behf_ctx* c, int kind, int ix, int iy, int iz, const float* w, int nt) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    if (kind < BEHF_SRC_EXPLOSIVE || kind > BEHF_SRC_FORCE_Z) return fail(BEHF_ERR_INVALID, "bad source kind %d", kind);
+    const int R = c->g.R;
+    const int ijk[3] = {ix, iy, iz}, n3[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+    for (int a = 0; a < 3; a++)
+        if (ijk[a] < R || ijk[a] >= n3[a] - R)
+            return fail(BEHF_ERR_INVALID, "source axis %d index %d outside the updated cells [%d,%d)", a, ijk[a], R,
+                        n3[a] - R);
+    if (nt < 0 || (nt > 0 && !w)) return fail(BEHF_ERR_INVALID, "bad wavelet");
+    if (c->d_wavelet) {
+        c->dfree(c->d_wavelet);
+        c->d_wavelet = nullptr;
+    }
+    behf_status st = c->dalloc((void**)&c->d_wavelet, align256((size_t)(nt > 0 ? nt : 1) * 4));
+    if (st) return st;
+    if (nt > 0) CK(cudaMemcpy(c->d_wavelet, w, (size_t)nt * 4, cudaMemcpyHostToDevice));
+    c->nw = nt;
+    c->src_kind = kind;
+    for (int a = 0; a < 3; a++) c->src_ijk[a] = ijk[a];
+    c->src_set = true;
+    c->invalidate_graph();
+    return BEHF_OK;
+}
+
+behf_status behf_set_receivers(behf_ctx* c, int nrec, const int* ijk, const int* comp, int capacity) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    if (nrec < 0 || capacity < 0 || (nrec > 0 && (!ijk || !comp)))
+        return fail(BEHF_ERR_INVALID, "bad receiver arguments");
+    std::vector<long long> off(nrec);
+    const int n3[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+    for (int r = 0; r < nrec; r++) {
+        for (int a = 0; a < 3; a++)
+            if (ijk[3 * r + a] < 0 || ijk[3 * r + a] >= n3[a])
+                return fail(BEHF_ERR_INVALID, "receiver %d axis %d index %d out of the grid", r, a, ijk[3 * r + a]);
+        if (comp[r] < 0 || comp[r] >= kNField) return fail(BEHF_ERR_INVALID, "receiver %d: bad field %d", r, comp[r]);
+        off[r] = c->cell_offset(ijk[3 * r], ijk[3 * r + 1], ijk[3 * r + 2]);
+    }
+    c->dfree(c->d_rec_off);
+    c->dfree(c->d_rec_comp);
+    c->dfree(c->d_seis);
+    c->d_rec_off = nullptr;
+    c->d_rec_comp = nullptr;
+    c->d_seis = nullptr;
+    c->nrec = 0;
+    c->cap = 0;
+    if (nrec > 0) {
+        behf_status st = c->dalloc((void**)&c->d_rec_off, align256((size_t)nrec * 8));
+        if (!st) st = c->dalloc((void**)&c->d_rec_comp, align256((size_t)nrec * 4));
+        if (!st) st = c->dalloc((void**)&c->d_seis, align256((size_t)nrec * (capacity > 0 ? capacity : 1) * 8));
+        if (st) return st;
+        CK(cudaMemcpy(c->d_rec_off, off.data(), (size_t)nrec * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->d_rec_comp, comp, (size_t)nrec * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemset(c->d_seis, 0, (size_t)nrec * (capacity > 0 ? capacity : 1) * 8));
+        c->nrec = nrec;
+        c->cap = capacity;
+    }
+    c->invalidate_graph();
+    return BEHF_OK;
+}
+
+behf_status behf_run_async(behf_ctx* c, int nsteps) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_run");
+    if (nsteps < 0) return fail(BEHF_ERR_INVALID, "negative step count");
+    if (c->nrec > 0 && c->step + nsteps > c->cap)
+        return fail(BEHF_ERR_INVALID, "receiver capacity %d exceeded (step %lld + %d)", c->cap, c->step, nsteps);
+    int left = nsteps;
+    double fac = 0;
+    CK(source_factor(c, &fac));
+    if (c->chunk > 0 && left >= c->chunk) {
+        if (!c->gexec) {
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue_steps(c, c->chunk, fac);
+            cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                return fail(BEHF_ERR_CUDA, "graph capture failed: %s",
+                            cudaGetErrorString(e != cudaSuccess ? e : e2));
+            }
+            e = cudaGraphInstantiate(&c->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                c->gexec = nullptr;
+                return fail(BEHF_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+            }
+        }
+        while (left >= c->chunk) {
+            CK(cudaGraphLaunch(c->gexec, c->stream));
+            left -= c->chunk;
+        }
+    }
+    if (left > 0) CK(enqueue_steps(c, left, fac));
+    c->step += nsteps;
+    return BEHF_OK;
+}
+
+behf_status behf_sync(behf_ctx* c) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return BEHF_OK;
+}
+
+behf_status behf_run(behf_ctx* c, int nsteps) {
+    behf_status st = behf_run_async(c, nsteps);
+    if (st) return st;
+    return behf_sync(c);
+}
+
+behf_status behf_get_seismograms(behf_ctx* c, double* out, int* nrec_steps) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    const int ns = (int)(c->step < c->cap ? c->step : c->cap);
+    if (nrec_steps) *nrec_steps = ns;
+    if (!out || c->nrec == 0) return BEHF_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    if (ns == c->cap) {
+        CK(cudaMemcpy(out, c->d_seis, (size_t)c->nrec * c->cap * 8, cudaMemcpyDeviceToHost));
+    } else if (ns > 0) {
+        CK(cudaMemcpy2D(out, (size_t)ns * 8, c->d_seis, (size_t)c->cap * 8, (size_t)ns * 8, c->nrec,
+                        cudaMemcpyDeviceToHost));
+    }
+    return BEHF_OK;
+}
+
+static behf_status field_io(behf_ctx* c, int q, float* host, bool get) {
+    if (!c || !host) return fail(BEHF_ERR_INVALID, "null argument");
+    if (q < 0 || q >= kNField) return fail(BEHF_ERR_INVALID, "bad field %d", q);
+    const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
+    float* tmp = nullptr;
+    behf_status st = c->dalloc((void**)&tmp, N * 4);
+    if (st) return st;
+    cudaError_t e = cudaSuccess;
+    const double sc = c->field_scale(q);
+    const Geom& g = c->g;
+    if (!get) e = cudaMemcpyAsync(tmp, host, N * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        switch (c->prec) {
+            case BEHF_FP64: e = get ? aux_get<double>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream)
+                                    : aux_set<double>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream); break;
+            case BEHF_FP32: e = get ? aux_get<float>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream)
+                                    : aux_set<float>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream); break;
+            case BEHF_FP16: e = get ? aux_get<__half>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream)
+                                    : aux_set<__half>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream); break;
+            default: e = get ? aux_get<__nv_bfloat16>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream)
+                             : aux_set<__nv_bfloat16>(c->p.f[q], tmp, g.nx, g.ny, g.nz, g.px, g.plane, sc, c->stream);
+        }
+    }
+    if (e == cudaSuccess && get) e = cudaMemcpyAsync(host, tmp, N * 4, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e2 = cudaStreamSynchronize(c->stream);
+    c->dfree(tmp);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(BEHF_ERR_CUDA, "field transfer failed: %s", cudaGetErrorString(e));
+    return BEHF_OK;
+}
+
+behf_status behf_get_field(behf_ctx* c, int q, float* out) { return field_io(c, q, out, true); }
+behf_status behf_set_field(behf_ctx* c, int q, const float* in) { return field_io(c, q, const_cast<float*>(in), false); }
+
+behf_status behf_reset(behf_ctx* c) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    return zero_state(c);
+}
+
+behf_status behf_set_option(behf_ctx* c, int opt, int value) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    switch (opt) {
+        case BEHF_OPT_KERNEL:
+            if (value < BEHF_KERNEL_AUTO || value > BEHF_KERNEL_TILED) return fail(BEHF_ERR_INVALID, "bad kernel %d", value);
+            if (value == BEHF_KERNEL_TILED) {
+                bool ok = false;
+                switch (c->prec) {
+                    case BEHF_FP64: ok = tiled_supported<double>(c->g); break;
+                    case BEHF_FP32: ok = tiled_supported<float>(c->g); break;
+                    case BEHF_FP16: ok = tiled_supported<__half>(c->g); break;
+                    case BEHF_BF16: ok = tiled_supported<__nv_bfloat16>(c->g); break;
+                }
+                if (!ok) return fail(BEHF_ERR_UNSUPPORTED, "tiled kernel not available for this precision/radius/grid");
+            }
+            c->kernel_opt = value;
+            break;
+        case BEHF_OPT_REF_BUG_COMPAT: c->g.bug = value ? 1 : 0; break;
+        case BEHF_OPT_GRAPH_CHUNK:
+            if (value < 0) return fail(BEHF_ERR_INVALID, "negative chunk");
+            c->chunk = value;
+            break;
+        default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
+    }
+    c->invalidate_graph();
+    return BEHF_OK;
+}
+
+behf_status behf_get_info(behf_ctx* c, behf_info* out) {
+    if (!c || !out) return fail(BEHF_ERR_INVALID, "null argument");
+    out->step = c->step;
+    out->device_bytes = c->device_bytes;
+    for (int s = 0; s < 4; s++) out->scales[s] = c->scales[s];
+    // algorithmic bytes per cell update: 13 fields read + written, 23 coefficients read, CPML memory
+    // (8 derivatives x {psi, prev} x read+write) on the slab fraction of each axis
+    const double n3[3] = {(double)c->grid.nx, (double)c->grid.ny, (double)c->grid.nz};
+    double cpml = 0;
+    for (int a = 0; a < 3; a++) cpml += c->g.W > 0 ? 16.0 * 2.0 * c->ws * c->g.W / n3[a] : 0.0;
+    out->bytes_per_cell = 26.0 * c->es + 3.0 * c->ws + 20.0 * c->ks + cpml;
+    bool tiled = false;
+    switch (c->prec) {
+        case BEHF_FP64: tiled = tiled_supported<double>(c->g); break;
+        case BEHF_FP32: tiled = tiled_supported<float>(c->g); break;
+        case BEHF_FP16: tiled = tiled_supported<__half>(c->g); break;
+        case BEHF_BF16: tiled = tiled_supported<__nv_bfloat16>(c->g); break;
+    }
+    out->kernel = (c->kernel_opt != BEHF_KERNEL_PLAIN && tiled) ? BEHF_KERNEL_TILED : BEHF_KERNEL_PLAIN;
+    out->radius = c->g.R;
+    out->precision = c->prec;
+    return BEHF_OK;
+}
+
+behf_status behf_get_stream(behf_ctx* c, void** s) {
+    if (!c || !s) return fail(BEHF_ERR_INVALID, "null argument");
+    *s = (void*)c->stream;
+    return BEHF_OK;
+}
+
+behf_status behf_health(behf_ctx* c, double* norms) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    const double limit = c->prec == BEHF_FP16 ? 65504.0 : c->prec == BEHF_FP64 ? 1.7976931348623157e308 : 3.4028234663852886e38;
+    const Geom& g = c->g;
+    CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+    for (int q = 0; q < kNField; q++) {
+        cudaError_t e;
+        switch (c->prec) {
+            case BEHF_FP64: e = aux_health<double>(c->p.f[q], g.nx, g.ny, g.nz, g.px, g.plane, limit, c->d_part, c->nblk_health, c->d_flag, c->d_norm + q, c->stream); break;
+            case BEHF_FP32: e = aux_health<float>(c->p.f[q], g.nx, g.ny, g.nz, g.px, g.plane, limit, c->d_part, c->nblk_health, c->d_flag, c->d_norm + q, c->stream); break;
+            case BEHF_FP16: e = aux_health<__half>(c->p.f[q], g.nx, g.ny, g.nz, g.px, g.plane, limit, c->d_part, c->nblk_health, c->d_flag, c->d_norm + q, c->stream); break;
+            default: e = aux_health<__nv_bfloat16>(c->p.f[q], g.nx, g.ny, g.nz, g.px, g.plane, limit, c->d_part, c->nblk_health, c->d_flag, c->d_norm + q, c->stream);
+        }
+        if (e != cudaSuccess) return fail(BEHF_ERR_CUDA, "health kernel: %s", cudaGetErrorString(e));
+    }
+    double h[kNField];
+    int flag = 0;
+    CK(cudaMemcpyAsync(h, c->d_norm, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (norms) std::memcpy(norms, h, sizeof h);
+    if (flag) return fail(BEHF_ERR_NONFINITE, "a field holds NaN/Inf or saturates its storage format");
+    return BEHF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+// behf_internal.cuh -- types shared by the libbehf translation units.
+//
+// Data layout in HBM (one context):
+//   * 13 wavefields, one array each, x fastest with a row pitch px (multiple of 16 elements) and
+//     plane stride px*ny; storage type S = double | float | __half | __nv_bfloat16, values scaled by
+//     the per-field storage scales (s_v for v, s_q for q, s_sigma for the stresses, s_p for p).
+//   * 23 per-cell coefficient arrays (same pitch): the three Darcy factors VW1 in W (float, or double
+//     for FP64) and 20 more in K (half for the 16-bit kinds, else S) multiplied by a power of two
+//     kmul[j] so that each array's largest magnitude sits just below 1.
+//   * CPML memory only inside the boundary slabs: for each axis 8 derivatives x {psi, previous
+//     derivative} in W, slab width W = 2L+1 cells ([0,L) and [n-1-L, n)), layouts
+//     x: [nz][ny][W], y: [nz][W][nx], z: [W][ny][nx].  The reference keeps 24+24 full-volume
+//     FP16 arrays instead (common.h:27-30).
+//   * 1-D damping profiles per axis (A = e, B = -dt d / 2, and the half-shifted A2, B2).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "behf.h"
+
+namespace behf {
+
+constexpr int kNField = 13;
+constexpr int kNCoef = 23;
+constexpr int kNMod = 9;
+
+// Coefficient indices (reference names VelocityWParameter*, VelocityUParameter*, PressParameter*,
+// StressParameter*: main.cpp:431-494).
+enum {
+    VW1X = 0, VW1Y, VW1Z, VW2X, VW2Y, VW2Z, VW3X, VW3Y, VW3Z, VU1X, VU1Y, VU1Z, VU2X, VU2Y, VU2Z,
+    P1, P2, S1, S2, S3, SXYC, SXZC, SYZC
+};
+
+// Storage traits: S stored, C arithmetic, K coefficient storage, W CPML memory / Darcy factor.
+template <class S> struct Traits;
+template <> struct Traits<double> {
+    typedef double C;
+    typedef double K;
+    typedef double W;
+    static __device__ __forceinline__ C ld(double v) { return v; }
+    static __device__ __forceinline__ double st(C v) { return v; }
+    static __device__ __forceinline__ C ldk(double v) { return v; }
+    static constexpr int prec = BEHF_FP64;
+};
+template <> struct Traits<float> {
+    typedef float C;
+    typedef float K;
+    typedef float W;
+    static __device__ __forceinline__ C ld(float v) { return v; }
+    static __device__ __forceinline__ float st(C v) { return v; }
+    static __device__ __forceinline__ C ldk(float v) { return v; }
+    static constexpr int prec = BEHF_FP32;
+};
+template <> struct Traits<__half> {
+    typedef float C;
+    typedef __half K;
+    typedef float W;
+    static __device__ __forceinline__ C ld(__half v) { return __half2float(v); }
+    static __device__ __forceinline__ __half st(C v) { return __float2half_rn(v); }
+    static __device__ __forceinline__ C ldk(__half v) { return __half2float(v); }
+    static constexpr int prec = BEHF_FP16;
+};
+template <> struct Traits<__nv_bfloat16> {
+    typedef float C;
+    typedef __half K;
+    typedef float W;
+    static __device__ __forceinline__ C ld(__nv_bfloat16 v) { return __bfloat162float(v); }
+    static __device__ __forceinline__ __nv_bfloat16 st(C v) { return __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ C ldk(__half v) { return __half2float(v); }
+    static constexpr int prec = BEHF_BF16;
+};
+
+// Staggered first-derivative weights of order 2R: D(i+1/2) = sum_m w_m (f[i+m] - f[i-m+1]) / h.
+template <int R>
+__host__ __device__ constexpr double stencil_w(int m) {
+    return R == 1 ? 1.0
+         : R == 2 ? (m == 1 ? 9.0 / 8.0 : -1.0 / 24.0)
+         : R == 3 ? (m == 1 ? 75.0 / 64.0 : m == 2 ? -25.0 / 384.0 : 3.0 / 640.0)
+                  : (m == 1 ? 1225.0 / 1024.0 : m == 2 ? -245.0 / 3072.0 : m == 3 ? 49.0 / 5120.0 : -5.0 / 7168.0);
+}
+
+// Type-erased device pointers of one context (cast inside the kernels).
+struct DevPtrs {
+    void* f[kNField];
+    void* k[kNCoef];       // k[0..2]: VW1 in W; k[3..22]: K
+    void* psi[3][8];       // CPML memory per axis, 4 V derivatives then 4 T derivatives
+    void* prv[3][8];
+    void* pa[3];           // per-axis profiles in C: e, -dt d/2 (integer points), and half-shifted
+    void* pb[3];
+    void* pa2[3];
+    void* pb2[3];
+};
+
+struct Geom {
+    int nx, ny, nz;
+    int R, L, W;           // stencil half-width, CPML width, slab width 2L+1 (0 without CPML)
+    long long px, plane;   // row pitch and plane stride in elements
+    int bug;               // reference vz/VW3y compatibility
+    float kmulf[kNCoef];   // power-of-two multipliers of the stored coefficients
+    double kmuld[kNCoef];
+};
+
+__host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
+    return i < L ? i : (i >= n - 1 - L ? L + (i - (n - 1 - L)) : -1);
+}
+
+// Launchers (defined per translation unit).
+template <class S> cudaError_t launch_plain(const Geom& g, const DevPtrs& p, bool vel, cudaStream_t st);
+template <class S> cudaError_t launch_tiled(const Geom& g, const DevPtrs& p, bool vel, cudaStream_t st);
+template <class S> bool tiled_supported(const Geom& g);
+
+}  // namespace behf

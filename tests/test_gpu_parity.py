@@ -1,0 +1,179 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the same inputs.
+
+Tolerances (seismogram relative L2 per field against the FP64 oracle of the same scheme):
+    FP64 storage  1e-10   (same arithmetic, FMA contraction only)
+    FP32 storage  1e-4    (the FP32 bar)
+    FP16 storage  2e-2    (the FP16 bar), and 5e-3 against the oracle's FP16-storage emulation
+    BF16 storage  0.15    (reported; 8-bit mantissas are outside the FP16 bar)
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f64": 1e-10, "f32": 1e-4, "f16": 2e-2, "bf16": 0.15}
+
+
+def _problem(n=30, nt=120, radius=4, cpml=6, kind="explosive"):
+    from behf import problems
+    p = problems.small64(n=n, nt=nt, radius=radius, cpml=cpml)
+    p.src_kind = kind
+    return p
+
+
+def _per_field_err(oracle, prob, a, b):
+    out = {}
+    for comp in np.unique(prob.rec_comp):
+        sel = prob.rec_comp == comp
+        out[int(comp)] = oracle.rel_l2(a[sel], b[sel])
+    return out
+
+
+def _run_gpu(prob, precision, kernel="auto", chunk=None, scales=None):
+    import behf
+    s = behf.solver_for(prob, precision=precision, kernel=kernel, scales=scales)
+    if chunk is not None:
+        s.set_option(behf.OPT_GRAPH_CHUNK, chunk)
+    s.run(prob.nt)
+    seis = s.seismograms()
+    info = s.info()
+    return s, seis, info
+
+
+@pytest.mark.parametrize("radius", [1, 2, 4])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_wide_precisions_match_oracle(behf_lib, oracle, radius, precision):
+    prob = _problem(radius=radius)
+    ref, _ = oracle.run(prob, "f64")
+    s, seis, info = _run_gpu(prob, precision)
+    assert seis.shape == ref.shape
+    errs = _per_field_err(oracle, prob, seis, ref)
+    assert max(errs.values()) < TOL[precision], errs
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["f16", "bf16"])
+def test_half_precisions_match_oracle(behf_lib, oracle, precision):
+    prob = _problem(n=32, nt=160)
+    ref, _ = oracle.run(prob, "f64")
+    s, seis, info = _run_gpu(prob, precision)
+    errs = _per_field_err(oracle, prob, seis, ref)
+    assert max(errs.values()) < TOL[precision], errs
+    s.close()
+
+
+def test_fp16_matches_oracle_storage_emulation(behf_lib, oracle):
+    """The GPU FP16 run follows the oracle's FP16-storage emulation (same scales, same rounding points)."""
+    prob = _problem(n=24, nt=80)
+    s, seis, info = _run_gpu(prob, "f16")
+    prob.scales = info["scales"]
+    emu, _ = oracle.run(prob, "f16")
+    ref, _ = oracle.run(prob, "f64")
+    e_emu = _per_field_err(oracle, prob, seis, emu)
+    e_ref = _per_field_err(oracle, prob, seis, ref)
+    assert max(e_emu.values()) < 5e-3, e_emu
+    assert max(e_emu.values()) < max(e_ref.values()), (e_emu, e_ref)
+    s.close()
+
+
+@pytest.mark.parametrize("kind", ["explosive", "pressure", "force_z"])
+def test_source_kinds(behf_lib, oracle, kind):
+    prob = _problem(n=26, nt=100, kind=kind)
+    ref, _ = oracle.run(prob, "f64")
+    s, seis, _ = _run_gpu(prob, "f32")
+    errs = _per_field_err(oracle, prob, seis, ref)
+    assert np.abs(ref).max() > 0
+    assert max(errs.values()) < 1e-4, errs
+    s.close()
+
+
+def test_final_wavefields_match(behf_lib, oracle):
+    import behf
+    prob = _problem(n=26, nt=60)
+    _, fields = oracle.run(prob, "f64", want_fields=True)
+    s = behf.solver_for(prob, precision="f32")
+    s.run(prob.nt)
+    for q, name in enumerate(behf.FIELDS):
+        g = s.get_field(name)
+        err = oracle.rel_l2(g, fields[q])
+        assert err < 1e-4, (name, err)
+    s.close()
+
+
+def test_reference_layout_problem(behf_lib, oracle):
+    """Radius 1, the reference's scales and the vz/VW3y compatibility, heterogeneous medium."""
+    from behf import problems
+    from conftest import load_golden
+    g = load_golden("ref_rock")
+    nz, ny, nx = (int(v) for v in g["shape"])
+    rl = g["rec_lin"].astype(np.int64)
+    ijk = np.stack([rl % nx, (rl // nx) % ny, rl // (nx * ny)], 1).astype(np.int32)
+    prob = problems.Problem(nx, ny, nz, float(g["h"]), float(g["dt"]), 1, g["medium"], g["wavelet"],
+                            tuple(int(v) for v in g["src"]), ijk, g["rec_comp"], cpml_width=int(g["np_cells"]),
+                            cpml_v0=4000.0, ref_bug_compat=True, scales=(1e8, 1e8, 1.0, 1.0), f0=1e4)
+    ref, _ = oracle.run(prob, "f64")
+    for prec, tol in (("f32", 1e-4), ("f16", 2e-2)):
+        _, seis, _ = _run_gpu(prob, prec, scales=prob.scales)
+        errs = _per_field_err(oracle, prob, seis, ref)
+        assert max(errs.values()) < tol, (prec, errs)
+    # and against the reference kernels themselves (golden, FP16 everywhere): same physics
+    _, seis16, _ = _run_gpu(prob, "f16", scales=prob.scales)
+    scale = np.array([1e8 if c < 6 else 1.0 for c in g["rec_comp"]])[:, None]
+    errs = _per_field_err(oracle, prob, seis16 * scale, g["seis"].astype(np.float64))
+    assert max(errs.values()) < 5e-2, errs
+
+
+def test_graph_and_direct_launch_identical(behf_lib):
+    prob = _problem(n=24, nt=50)
+    _, a, _ = _run_gpu(prob, "f16", chunk=0)
+    _, b, _ = _run_gpu(prob, "f16", chunk=16)
+    _, c, _ = _run_gpu(prob, "f16", chunk=7)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+
+
+def test_split_runs_equal_one_run(behf_lib):
+    import behf
+    prob = _problem(n=24, nt=64)
+    s = behf.solver_for(prob, precision="f32")
+    s.run(64)
+    one = s.seismograms()
+    s.reset()
+    for n in (5, 16, 20, 23):
+        s.run(n)
+    np.testing.assert_array_equal(one, s.seismograms())
+    s.close()
+
+
+def test_field_roundtrip_and_health(behf_lib):
+    import behf
+    prob = _problem(n=20, nt=10)
+    s = behf.solver_for(prob, precision="f32")
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(s.shape).astype(np.float32)
+    s.set_field("szz", v)
+    np.testing.assert_array_equal(s.get_field("szz"), v)
+    ok, norms = s.health()
+    assert ok and norms[behf.FIELD["szz"]] == pytest.approx(float(np.sum(v.astype(np.float64) ** 2)), rel=1e-12)
+    v[3, 4, 5] = np.inf
+    s.set_field("szz", v)
+    ok, _ = s.health()
+    assert not ok
+    s.close()
+
+
+def test_errors_are_reported_not_fatal(behf_lib):
+    import behf
+    with pytest.raises(behf.BehfError):
+        behf.Solver(4, 30, 30, 5.0, 4e-4, radius=4, precision="f32", cpml_width=0)
+    s = behf.Solver(20, 20, 20, 5.0, 4e-4, radius=2, precision="f16", cpml_width=4)
+    with pytest.raises(behf.BehfError) as e:
+        s.run(1)
+    assert e.value.code == -4
+    with pytest.raises(behf.BehfError):
+        s.set_source("explosive", (0, 5, 5), np.ones(4, np.float32))
+    with pytest.raises(behf.BehfError):
+        s.set_receivers(np.array([[1, 2, 30]]), np.array([0]), 10)
+    with pytest.raises(behf.BehfError):
+        s.set_receivers(np.array([[1, 2, 3]]), np.array([13]), 10)
+    s.close()
