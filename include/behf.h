@@ -75,6 +75,7 @@ typedef struct {
     double bytes_per_cell;   /* algorithmic HBM bytes of one cell update (state + coefficients + CPML) */
     int kernel;              /* kernel family in use (behf_kernel) */
     int radius, precision;
+    int64_t launches;        /* kernels enqueued by this context so far (graph launches count their nodes) */
 } behf_info;
 
 /* Kernel family: PLAIN = one thread per cell with cached neighbour loads; TILED = the z-marching
@@ -100,6 +101,32 @@ behf_status behf_set_medium(behf_ctx* ctx, const float* const moduli[BEHF_NMOD])
 /* Same, from device arrays (not freed, not kept). */
 behf_status behf_set_medium_device(behf_ctx* ctx, const float* const moduli[BEHF_NMOD]);
 
+/* Synthetic media generated on the device (no host volumes).  A rock is the parameter set of the
+ * reference's create_model_all (outputfunc.cpp:153-222); phi >= 1 marks pure fluid. */
+typedef struct {
+    double Ks, Kf, Kdry, mu, rhos, rhof, phi, kappa, eta, tau;
+} behf_rock;
+
+typedef struct {
+    int nlayers;                 /* 1..4 layers in z */
+    behf_rock layers[4];
+    int interface_z[3];          /* layer l spans [interface_z[l-1], interface_z[l]) cells */
+    int seed;                    /* perturbation seed (0 .. 2^20-1) */
+    double corr_cells;           /* correlation length exp(-r^2/l^2) in cells */
+    double pct;                  /* relative std of K_dry, mu, phi (0 = no perturbation) */
+    double log_kappa_sigma;      /* std of ln kappa */
+    int anomaly;                 /* 1: Gaussian anomaly exp(-r^2/R^2) */
+    double anom_center[3];       /* cell coordinates (x, y, z) */
+    double anom_radius_cells;
+    double anom_dkdry;           /* K_dry *= 1 + anom_dkdry G */
+    double anom_kappa_factor;    /* kappa *= anom_kappa_factor^G */
+} behf_medium_spec;
+
+/* Build the moduli of a synthetic medium on the device, then the coefficients (as behf_set_medium).
+ * The noise is splitmix64-hashed per (cell, field, seed), Box-Muller in FP64, smoothed by a periodic
+ * separable Gaussian of std l/2 and scaled to unit variance. */
+behf_status behf_generate_medium(behf_ctx* ctx, const behf_medium_spec* spec);
+
 /* Explicit 1-D CPML profiles for one axis (0 = x, 1 = y, 2 = z), n entries each: damping d at the
  * integer points and d2 at the half-shifted points (1/s).  Overrides the profile built from
  * cpml_width/v0/r (main.cpp:519-1371).  Call before behf_set_medium or behf_reset. */
@@ -119,6 +146,17 @@ behf_status behf_set_receivers(behf_ctx* ctx, int nrec, const int* ijk, const in
 behf_status behf_run(behf_ctx* ctx, int nsteps);
 behf_status behf_run_async(behf_ctx* ctx, int nsteps);
 behf_status behf_sync(behf_ctx* ctx);
+
+/* Replace wavelet samples [it0, it0+n) (host, copied; extends the wavelet if needed).  With
+ * behf_get_seismograms_range this streams a run step by step from and to host memory. */
+behf_status behf_update_wavelet(behf_ctx* ctx, int it0, const float* w, int n);
+/* Seismogram columns [it0, it0+n) of every receiver, physical units, [nrec][n] into out (host). */
+behf_status behf_get_seismograms_range(behf_ctx* ctx, int it0, int n, double* out);
+
+/* Advance nsteps with direct launches, timing every launch with CUDA events on the context's
+ * stream; ms[4] receives the mean duration (ms) of the source, velocity, stress and receiver
+ * kernels.  For roofline accounting. */
+behf_status behf_time_kernels(behf_ctx* ctx, int nsteps, double* ms);
 
 /* Seismograms recorded so far, physical units, [nrec][nsteps_recorded] into out (host). */
 behf_status behf_get_seismograms(behf_ctx* ctx, double* out, int* nsteps_recorded);

@@ -38,9 +38,42 @@ class Grid(C.Structure):
                 ("scales", C.c_double * 4), ("src_amp_hint", C.c_double), ("src_f0_hint", C.c_double)]
 
 
+class Rock(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("Ks", "Kf", "Kdry", "mu", "rhos", "rhof", "phi", "kappa", "eta", "tau")]
+
+
+class MediumSpec(C.Structure):
+    _fields_ = [("nlayers", C.c_int), ("layers", Rock * 4), ("interface_z", C.c_int * 3), ("seed", C.c_int),
+                ("corr_cells", C.c_double), ("pct", C.c_double), ("log_kappa_sigma", C.c_double),
+                ("anomaly", C.c_int), ("anom_center", C.c_double * 3), ("anom_radius_cells", C.c_double),
+                ("anom_dkdry", C.c_double), ("anom_kappa_factor", C.c_double)]
+
+
+def medium_spec(layers, interfaces=(), seed=1234, corr_cells=10.0, pct=0.0, log_kappa_sigma=0.0,
+                anomaly=None) -> MediumSpec:
+    """C struct of a synthetic medium (same arguments as behf.problems.spec_medium)."""
+    s = MediumSpec()
+    s.nlayers = len(layers)
+    for i, r in enumerate(layers):
+        for k, v in r.items():
+            setattr(s.layers[i], k, float(v))
+    for i, z in enumerate(interfaces):
+        s.interface_z[i] = int(z)
+    s.seed, s.corr_cells, s.pct, s.log_kappa_sigma = int(seed), float(corr_cells), float(pct), float(log_kappa_sigma)
+    if anomaly:
+        s.anomaly = 1
+        for i in range(3):
+            s.anom_center[i] = float(anomaly["center"][i])
+        s.anom_radius_cells = float(anomaly["radius"])
+        s.anom_dkdry = float(anomaly["dkdry"])
+        s.anom_kappa_factor = float(anomaly["kappa_factor"])
+    return s
+
+
 class Info(C.Structure):
     _fields_ = [("step", C.c_int64), ("device_bytes", C.c_int64), ("scales", C.c_double * 4),
-                ("bytes_per_cell", C.c_double), ("kernel", C.c_int), ("radius", C.c_int), ("precision", C.c_int)]
+                ("bytes_per_cell", C.c_double), ("kernel", C.c_int), ("radius", C.c_int), ("precision", C.c_int),
+                ("launches", C.c_int64)]
 
 
 def lib_path() -> Path:
@@ -61,6 +94,7 @@ def load() -> C.CDLL:
         "behf_destroy": [C.c_void_p],
         "behf_set_medium": [C.c_void_p, P(P(C.c_float))],
         "behf_set_medium_device": [C.c_void_p, P(C.c_void_p)],
+        "behf_generate_medium": [C.c_void_p, P(MediumSpec)],
         "behf_set_cpml_profile": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double)],
         "behf_set_source": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_float), C.c_int],
         "behf_set_receivers": [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), C.c_int],
@@ -75,6 +109,9 @@ def load() -> C.CDLL:
         "behf_get_info": [C.c_void_p, P(Info)],
         "behf_get_stream": [C.c_void_p, P(C.c_void_p)],
         "behf_health": [C.c_void_p, P(C.c_double)],
+        "behf_update_wavelet": [C.c_void_p, C.c_int, P(C.c_float), C.c_int],
+        "behf_get_seismograms_range": [C.c_void_p, C.c_int, C.c_int, P(C.c_double)],
+        "behf_time_kernels": [C.c_void_p, C.c_int, P(C.c_double)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -144,6 +181,11 @@ class Solver:
         arr = (C.c_void_p * 9)(*ptrs)
         _check(self._lib.behf_set_medium_device(self._ctx, arr))
 
+    def generate_medium(self, spec: dict):
+        """Device-side synthetic medium (spec: the arguments of behf.problems.spec_medium)."""
+        cs = medium_spec(**spec)
+        _check(self._lib.behf_generate_medium(self._ctx, C.byref(cs)))
+
     def set_cpml_profile(self, axis: int, d: np.ndarray, d2: np.ndarray):
         d = np.ascontiguousarray(d, np.float64)
         d2 = np.ascontiguousarray(d2, np.float64)
@@ -208,7 +250,24 @@ class Solver:
         _check(self._lib.behf_get_info(self._ctx, C.byref(inf)))
         return {"step": inf.step, "device_bytes": inf.device_bytes, "scales": tuple(inf.scales),
                 "bytes_per_cell": inf.bytes_per_cell, "kernel": {0: "auto", 1: "plain", 2: "tiled"}[inf.kernel],
-                "radius": inf.radius, "precision": inf.precision}
+                "radius": inf.radius, "precision": inf.precision, "launches": inf.launches}
+
+    def update_wavelet(self, it0: int, w: np.ndarray):
+        w = _f32(w)
+        _check(self._lib.behf_update_wavelet(self._ctx, int(it0), w.ctypes.data_as(C.POINTER(C.c_float)),
+                                             int(w.shape[0])))
+
+    def seismograms_range(self, it0: int, n: int, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros((self.nrec, n), np.float64)
+        _check(self._lib.behf_get_seismograms_range(self._ctx, int(it0), int(n),
+                                                    out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def time_kernels(self, nsteps: int) -> dict:
+        ms = np.zeros(4, np.float64)
+        _check(self._lib.behf_time_kernels(self._ctx, int(nsteps), ms.ctypes.data_as(C.POINTER(C.c_double))))
+        return {"source": ms[0], "velocity": ms[1], "stress": ms[2], "record": ms[3]}
 
     def health(self):
         norms = np.zeros(13, np.float64)
@@ -223,6 +282,26 @@ class Solver:
         return s.value or 0
 
 
+def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:
+    """Compulsory HBM bytes per cell update of each kernel and of a whole step.
+
+    velocity: reads 7 stresses/pressure + 6 v/q, writes 6 v/q; 3 FP32 Darcy factors + 12 coefficients;
+              CPML psi + previous derivative (FP32) read and written for its 4 derivatives per axis on
+              the slab fraction W/n of that axis (W = 2L+1).
+    stress:   reads 6 v/q + 7 stresses/pressure, writes 7; 8 coefficients; CPML as velocity.
+    step_fused: the per-step figure with each field read and written once (26 field accesses),
+              23 coefficients and the CPML memory -- the algorithmic bytes of one cell update."""
+    es = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}[precision]
+    ks = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}[precision]
+    ws = 8 if precision == "f64" else 4
+    W = 2 * cpml_width + 1 if cpml_width > 0 else 0
+    cpml_half = sum(4 * 2 * 2 * ws * W / n for n in shape)
+    vel = 19 * es + 3 * ws + 12 * ks + cpml_half
+    strs = 20 * es + 8 * ks + cpml_half
+    fused = 26 * es + 3 * ws + 20 * ks + 2 * cpml_half
+    return {"velocity": vel, "stress": strs, "step_unfused": vel + strs, "step_fused": fused}
+
+
 def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None) -> Solver:
     """A Solver set up with a problem description (see behf.problems.Problem)."""
     s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
@@ -232,7 +311,10 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None)
     if prob.ref_bug_compat:
         s.set_option(OPT_REF_BUG_COMPAT, 1)
     s.set_kernel(kernel)
-    s.set_medium(prob.mod)
+    if prob.mod.shape[1:] == (prob.nz, prob.ny, prob.nx):
+        s.set_medium(prob.mod)
+    else:
+        s.generate_medium(prob.extra["spec"])
     s.set_source(prob.src_kind, prob.src, prob.wavelet)
     if len(prob.rec_comp):
         s.set_receivers(prob.rec_ijk, prob.rec_comp, prob.nt if capacity is None else capacity)

@@ -60,24 +60,77 @@ def p_velocity(rock: dict) -> float:
     return float(np.sqrt(m[5] / m[0]))
 
 
-def gaussian_random_field(shape, corr_cells: float, seed: int) -> np.ndarray:
-    """Zero-mean, unit-variance field with correlation exp(-r^2 / l^2), l = corr_cells (float64).
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    x = x + np.uint64(0x9E3779B97F4A7C15)
+    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
 
-    White noise smoothed by a separable Gaussian of std l/2 (periodic wrap), normalised by the
-    filter's analytic gain sqrt(sum g^2)^3."""
-    rng = np.random.default_rng(seed)
-    f = rng.standard_normal(shape)
+
+def hash_noise(n_cells: int, f: int, seed: int) -> np.ndarray:
+    """Standard normal samples, one per cell: Box-Muller (FP64) on two 24-bit fields of
+    splitmix64(cell | f << 32 | seed << 36); the device generator draws the same numbers."""
+    c = np.arange(n_cells, dtype=np.uint64) | (np.uint64(f) << np.uint64(32)) | (np.uint64(seed) << np.uint64(36))
+    with np.errstate(over="ignore"):
+        h = _splitmix64(c)
+    u1 = ((h >> np.uint64(40)).astype(np.float64) + 0.5) / 16777216.0
+    u2 = (((h >> np.uint64(16)) & np.uint64(0xFFFFFF)).astype(np.float64) + 0.5) / 16777216.0
+    return (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)).astype(np.float32)
+
+
+def gaussian_weights(corr_cells: float):
     sig = corr_cells / 2.0
     half = int(np.ceil(4 * sig))
     x = np.arange(-half, half + 1)
     g = np.exp(-0.5 * (x / sig) ** 2)
     g /= g.sum()
-    for ax in range(3):
-        acc = np.zeros_like(f)
-        for k, w in zip(x, g):
-            acc += w * np.roll(f, k, axis=ax)
-        f = acc
-    return f / np.sqrt(np.sum(g * g)) ** 3
+    return x, g
+
+
+def gaussian_random_field(shape, corr_cells: float, seed: int, f: int = 0) -> np.ndarray:
+    """Zero-mean, unit-variance field with correlation exp(-r^2 / l^2), l = corr_cells.
+
+    Hash noise smoothed by a separable Gaussian of std l/2 (periodic wrap, x then y then z, float32
+    accumulation), normalised by the filter's gain (sum w^2)^(3/2) -- the device generator's
+    algorithm (kernels_medium.cu)."""
+    n = int(np.prod(shape))
+    f32 = hash_noise(n, f, seed).reshape(shape)
+    x, g = gaussian_weights(corr_cells)
+    w = g.astype(np.float32)
+    for ax in (2, 1, 0):  # x, y, z of a [z][y][x] array
+        acc = np.zeros_like(f32)
+        for k, wk in zip(x, w):
+            acc += wk * np.roll(f32, int(k), axis=ax)
+        f32 = acc
+    return f32.astype(np.float64) * (1.0 / np.sqrt(np.sum(g * g)) ** 3)
+
+
+def spec_medium(shape, layers, interfaces=(), seed=1234, corr_cells=10.0, pct=0.0, log_kappa_sigma=0.0,
+                anomaly=None) -> np.ndarray:
+    """Host mirror of behf_generate_medium: layered rocks, correlated perturbations, Gaussian anomaly.
+
+    anomaly = dict(center=(x, y, z), radius=R_cells, dkdry=..., kappa_factor=...)."""
+    nz, ny, nx = shape
+    kk = np.arange(nz)[:, None, None] * np.ones((1, ny, nx))
+    layer = np.zeros(shape, np.int64)
+    for zi in interfaces:
+        layer += (kk >= zi)
+    keys = ("Ks", "Kf", "Kdry", "mu", "rhos", "rhof", "phi", "kappa", "eta", "tau")
+    par = {k: np.asarray([r[k] for r in layers], np.float64)[layer] for k in keys}
+    if pct != 0 or log_kappa_sigma != 0:
+        g = [gaussian_random_field(shape, corr_cells, seed, f) for f in range(4)]
+        par["Kdry"] = par["Kdry"] * (1 + pct * g[0])
+        par["mu"] = par["mu"] * (1 + pct * g[1])
+        par["phi"] = np.where(par["phi"] < 1.0, par["phi"] * (1 + pct * g[2]), par["phi"])
+        par["kappa"] = par["kappa"] * np.exp(log_kappa_sigma * g[3])
+    if anomaly:
+        ii = np.arange(nx)[None, None, :]
+        jj = np.arange(ny)[None, :, None]
+        cx, cy, cz = anomaly["center"]
+        G = np.exp(-((ii - cx) ** 2 + (jj - cy) ** 2 + (kk - cz) ** 2) / anomaly["radius"] ** 2)
+        par["Kdry"] = par["Kdry"] * (1 + anomaly["dkdry"] * G)
+        par["kappa"] = par["kappa"] * np.power(anomaly["kappa_factor"], G)
+    return rock_moduli(**par).astype(np.float32)
 
 
 @dataclass
@@ -156,13 +209,13 @@ def layered(shape, rocks, interfaces) -> np.ndarray:
 
 
 def random_medium(shape, rock=SANDSTONE, seed=1234, corr_cells=10.0, pct=0.05, log_kappa_sigma=0.5):
-    g = [gaussian_random_field(shape, corr_cells, seed + i) for i in range(4)]
-    p = dict(rock)
-    p["Kdry"] = rock["Kdry"] * (1 + pct * g[0])
-    p["mu"] = rock["mu"] * (1 + pct * g[1])
-    p["phi"] = rock["phi"] * (1 + pct * g[2])
-    p["kappa"] = rock["kappa"] * np.exp(log_kappa_sigma * g[3])
-    return rock_moduli(**p).astype(np.float32)
+    return spec_medium(shape, [rock], (), seed, corr_cells, pct, log_kappa_sigma)
+
+
+def random_spec(rock=SANDSTONE, seed=1234, corr_cells=10.0, pct=0.05, log_kappa_sigma=0.5) -> dict:
+    """The random1024 medium as a device-generator spec (see behf.Solver.generate_medium)."""
+    return dict(layers=[rock], interfaces=(), seed=seed, corr_cells=corr_cells, pct=pct,
+                log_kappa_sigma=log_kappa_sigma, anomaly=None)
 
 
 def line_receivers(ix, iy, iz, comps):
@@ -202,6 +255,7 @@ def random1024(n=1024, nt=3000, radius=4, cpml=20, nrec_side=512, seed=1234, med
     h, dt, f0 = 5.0, 4e-4, 20.0
     shape = (n, n, n)
     mod = random_medium(shape, seed=seed) if medium else np.zeros((9, 1, 1, 1), np.float32)
+    spec = random_spec(seed=seed)
     c = n // 2
     ax = np.linspace(cpml + 2, n - cpml - 3, nrec_side).round().astype(int)
     X, Y = np.meshgrid(ax, ax, indexing="xy")
@@ -209,7 +263,7 @@ def random1024(n=1024, nt=3000, radius=4, cpml=20, nrec_side=512, seed=1234, med
     src = (c, c, min(n // 4, n - cpml - 6))
     return Problem(n, n, n, h, dt, radius, mod, ricker(nt, dt, f0), src, ijk, comp, src_kind="force_z",
                    cpml_width=cpml, cpml_v0=p_velocity(SANDSTONE) * 1.1, f0=f0, name=f"random{n}",
-                   extra={"seed": seed})
+                   extra={"seed": seed, "spec": spec})
 
 
 def borehole_moduli(nz, ny, nx) -> np.ndarray:

@@ -10,6 +10,7 @@
 
 #include "behf_aux.cuh"
 #include "behf_internal.cuh"
+#include "behf_medium.cuh"
 
 using namespace behf;
 
@@ -98,6 +99,11 @@ struct behf_ctx {
     int chunk = 16;
     cudaGraphExec_t gexec = nullptr;
     int kernel_opt = BEHF_KERNEL_AUTO;
+    int64_t launches = 0;        // kernels enqueued (host count)
+    int64_t graph_nodes = 0;     // kernels per captured graph
+    cudaEvent_t* tev = nullptr;  // per-launch events when timing (2 per launch)
+    int tev_used = 0;
+    std::vector<int> tkind;
     // health scratch
     double* d_part = nullptr;
     int* d_flag = nullptr;
@@ -180,6 +186,24 @@ cudaError_t source_factor(behf_ctx* c, double* fac) {
     return cudaSuccess;
 }
 
+// Timing brackets: when c->tev is set, each launch of kind k is bracketed by events 2*i, 2*i+1 and
+// its kind recorded in c->tkind.
+struct TimedLaunch {
+    behf_ctx* c;
+    int kind;
+    TimedLaunch(behf_ctx* cc, int k) : c(cc), kind(k) {
+        if (c->tev) cudaEventRecord(c->tev[2 * c->tev_used], c->stream);
+    }
+    ~TimedLaunch() {
+        if (c->tev) {
+            cudaEventRecord(c->tev[2 * c->tev_used + 1], c->stream);
+            c->tkind.push_back(kind);
+            c->tev_used++;
+        }
+        c->launches++;
+    }
+};
+
 template <class S>
 cudaError_t enqueue_steps_t(behf_ctx* c, int n, double fac) {
     const long long so = c->src_set ? c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]) : 0;
@@ -188,19 +212,31 @@ cudaError_t enqueue_steps_t(behf_ctx* c, int n, double fac) {
     for (int s = 0; s < n; s++) {
         cudaError_t e;
         if (c->src_set && c->src_kind != BEHF_SRC_FORCE_Z) {
+            TimedLaunch t(c, 0);
             e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, s, fac, c->stream);
             if (e != cudaSuccess) return e;
         }
-        if ((e = dispatch_update(c, true)) != cudaSuccess) return e;
+        {
+            TimedLaunch t(c, 1);
+            if ((e = dispatch_update(c, true)) != cudaSuccess) return e;
+        }
         if (c->src_set && c->src_kind == BEHF_SRC_FORCE_Z) {
+            TimedLaunch t(c, 0);
             e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, s, fac, c->stream);
             if (e != cudaSuccess) return e;
         }
-        if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
-        if ((e = aux_record<S>(c->p, c->d_rec_off, c->d_rec_comp, c->nrec, c->d_seis, c->cap, c->d_it, s, rs,
-                               c->stream)) != cudaSuccess)
-            return e;
+        {
+            TimedLaunch t(c, 2);
+            if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
+        }
+        if (c->nrec > 0) {
+            TimedLaunch t(c, 3);
+            if ((e = aux_record<S>(c->p, c->d_rec_off, c->d_rec_comp, c->nrec, c->d_seis, c->cap, c->d_it, s, rs,
+                                   c->stream)) != cudaSuccess)
+                return e;
+        }
     }
+    c->launches++;
     return aux_tick(c->d_it, n, c->stream);
 }
 
@@ -512,6 +548,30 @@ behf_status behf_set_medium(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
     return st;
 }
 
+behf_status behf_generate_medium(behf_ctx* c, const behf_medium_spec* spec) {
+    if (!c || !spec) return fail(BEHF_ERR_INVALID, "null argument");
+    if (spec->nlayers < 1 || spec->nlayers > 4) return fail(BEHF_ERR_INVALID, "nlayers must be 1..4");
+    const bool noise = spec->pct != 0 || spec->log_kappa_sigma != 0;
+    if (noise && !(spec->corr_cells > 0)) return fail(BEHF_ERR_INVALID, "corr_cells must be positive");
+    if (spec->seed < 0 || spec->seed >= (1 << 20)) return fail(BEHF_ERR_INVALID, "seed must be in [0, 2^20)");
+    const long long N = (long long)c->grid.nx * c->grid.ny * c->grid.nz;
+    float* dm[kNMod] = {};
+    float* work = nullptr;
+    behf_status st = BEHF_OK;
+    for (int q = 0; q < kNMod && st == BEHF_OK; q++) st = c->dalloc((void**)&dm[q], (size_t)N * 4);
+    if (st == BEHF_OK && noise) st = c->dalloc((void**)&work, (size_t)N * 4 * 5);
+    if (st == BEHF_OK) {
+        cudaError_t e = generate_medium(*spec, c->grid.nx, c->grid.ny, c->grid.nz, dm, work, c->stream,
+                                        aux_grid_blocks());
+        if (e != cudaSuccess) st = fail(BEHF_ERR_CUDA, "medium generation failed: %s", cudaGetErrorString(e));
+    }
+    if (work) c->dfree(work);
+    if (st == BEHF_OK) st = set_medium_dev(c, dm);
+    cudaStreamSynchronize(c->stream);
+    for (int q = 0; q < kNMod; q++) c->dfree(dm[q]);
+    return st;
+}
+
 behf_status behf_set_cpml_profile(behf_ctx* c, int axis, const double* d, const double* d2) {
     if (!c || axis < 0 || axis > 2 || !d || !d2) return fail(BEHF_ERR_INVALID, "bad argument");
     const int n = axis == 0 ? c->grid.nx : axis == 1 ? c->grid.ny : c->grid.nz;
@@ -595,7 +655,10 @@ behf_status behf_run_async(behf_ctx* c, int nsteps) {
         if (!c->gexec) {
             cudaGraph_t graph = nullptr;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            const int64_t l0 = c->launches;
             cudaError_t e = enqueue_steps(c, c->chunk, fac);
+            c->graph_nodes = c->launches - l0;
+            c->launches = l0;
             cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
             if (e != cudaSuccess || e2 != cudaSuccess) {
                 if (graph) cudaGraphDestroy(graph);
@@ -611,6 +674,7 @@ behf_status behf_run_async(behf_ctx* c, int nsteps) {
         }
         while (left >= c->chunk) {
             CK(cudaGraphLaunch(c->gexec, c->stream));
+            c->launches += c->graph_nodes;
             left -= c->chunk;
         }
     }
@@ -734,6 +798,66 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
     out->kernel = (c->kernel_opt != BEHF_KERNEL_PLAIN && tiled) ? BEHF_KERNEL_TILED : BEHF_KERNEL_PLAIN;
     out->radius = c->g.R;
     out->precision = c->prec;
+    out->launches = c->launches;
+    return BEHF_OK;
+}
+
+behf_status behf_update_wavelet(behf_ctx* c, int it0, const float* w, int n) {
+    if (!c || (n > 0 && !w) || it0 < 0 || n < 0) return fail(BEHF_ERR_INVALID, "bad argument");
+    if (!c->src_set) return fail(BEHF_ERR_STATE, "behf_set_source must come first");
+    if (it0 + n > c->nw) {  // grow, keeping the old samples
+        float* nw = nullptr;
+        behf_status st = c->dalloc((void**)&nw, align256((size_t)(it0 + n) * 4));
+        if (st) return st;
+        CK(cudaMemsetAsync(nw, 0, (size_t)(it0 + n) * 4, c->stream));
+        if (c->nw > 0) CK(cudaMemcpyAsync(nw, c->d_wavelet, (size_t)c->nw * 4, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->dfree(c->d_wavelet);
+        c->d_wavelet = nw;
+        c->nw = it0 + n;
+        c->invalidate_graph();
+    }
+    if (n > 0) CK(cudaMemcpyAsync(c->d_wavelet + it0, w, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    return BEHF_OK;
+}
+
+behf_status behf_get_seismograms_range(behf_ctx* c, int it0, int n, double* out) {
+    if (!c || n < 0 || it0 < 0 || (n > 0 && !out)) return fail(BEHF_ERR_INVALID, "bad argument");
+    if (it0 + n > c->cap) return fail(BEHF_ERR_INVALID, "range beyond the receiver capacity %d", c->cap);
+    if (c->nrec == 0 || n == 0) return BEHF_OK;
+    CK(cudaMemcpy2DAsync(out, (size_t)n * 8, c->d_seis + it0, (size_t)c->cap * 8, (size_t)n * 8, c->nrec,
+                         cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return BEHF_OK;
+}
+
+behf_status behf_time_kernels(behf_ctx* c, int nsteps, double* ms) {
+    if (!c || !ms || nsteps <= 0) return fail(BEHF_ERR_INVALID, "bad argument");
+    if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before timing");
+    if (c->nrec > 0 && c->step + nsteps > c->cap) return fail(BEHF_ERR_INVALID, "receiver capacity exceeded");
+    const int maxl = 4 * nsteps;
+    std::vector<cudaEvent_t> ev(2 * maxl);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    double fac = 0;
+    CK(source_factor(c, &fac));
+    c->tev = ev.data();
+    c->tev_used = 0;
+    c->tkind.clear();
+    cudaError_t e = enqueue_steps(c, nsteps, fac);
+    c->tev = nullptr;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    double sum[4] = {0, 0, 0, 0};
+    int cnt[4] = {0, 0, 0, 0};
+    for (int i = 0; i < c->tev_used && e == cudaSuccess; i++) {
+        float t = 0;
+        e = cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]);
+        sum[c->tkind[i]] += t;
+        cnt[c->tkind[i]]++;
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return fail(BEHF_ERR_CUDA, "kernel timing failed: %s", cudaGetErrorString(e));
+    for (int k = 0; k < 4; k++) ms[k] = cnt[k] ? sum[k] / cnt[k] : 0.0;
+    c->step += nsteps;
     return BEHF_OK;
 }
 

@@ -102,6 +102,16 @@ static inline int slab_index(int i, int n, int L) {
     return -1;
 }
 
+static double g_step_seconds = 0.0;
+
+static double wall_seconds() {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
 static void set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);
@@ -533,7 +543,9 @@ struct Runner {
             force = cfg->dt / rz * sv;
         }
 
+        double t_start = wall_seconds();
         for (int it = 0; it < nt; it++) {
+            if (it == cfg->time_from_step) t_start = wall_seconds();
             const double w = wavelet[it];
             if (cfg->src_kind == ORC_SRC_EXPLOSIVE) {
                 for (int q = ORC_SXX; q <= ORC_SZZ; q++) f[q][src] = Pr::st(ld(q, src) + (C)(w * ss));
@@ -549,6 +561,7 @@ struct Runner {
                 seis[(size_t)r * nt + it] = (double)ld(q, o) / fscale[q];
             }
         }
+        g_step_seconds = wall_seconds() - t_start;
         if (fields_out) {
             for (int q = 0; q < ORC_NFIELD; q++)
                 for (size_t c = 0; c < N; c++) fields_out[(size_t)q * N + c] = (double)ld(q, c) / fscale[q];
@@ -570,6 +583,16 @@ int run_p(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* w, 
 }
 
 }  // namespace
+
+extern "C" double orc_last_step_seconds(void) { return g_step_seconds; }
+
+extern "C" int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
 
 extern "C" int orc_run(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
                        int nrec, const int* rec_ijk, const int* rec_comp, double* seis, double* fields_out) {

@@ -58,6 +58,7 @@ typedef struct {
     int src_kind, src_ix, src_iy, src_iz;
     double src_factor;       /* FORCE_Z only: velocity increment per unit wavelet (dt/rho_z) */
     int nthreads;            /* OpenMP threads (<=0: all) */
+    int time_from_step;      /* orc_last_step_seconds covers steps [time_from_step, nt) */
 } orc_cfg;
 
 /* Reference borehole medium (outputfunc.cpp:153-222), cell-centred, float [nz][ny][nx]. */
@@ -85,6 +86,10 @@ void orc_ricker(int nt, double dt, double f0, double t0, double amp, float* w);
  * Returns 0 on success, negative on invalid input. */
 int orc_run(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
             int nrec, const int* rec_ijk, const int* rec_comp, double* seis, double* fields_out);
+
+/* Wall seconds of the time-step loop of the last orc_run (set-up excluded); OpenMP thread count. */
+double orc_last_step_seconds(void);
+int orc_threads(void);
 
 /* Reference-arithmetic run (radius 1, FP16 everywhere).  All arrays are [nz][ny][nx] binary16
  * bit patterns.  state[16]: the 13 fields in field order, then vwx2, vwy2, vwz2.

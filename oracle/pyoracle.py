@@ -31,7 +31,7 @@ class OrcCfg(C.Structure):
         ("cpml_width", C.c_int), ("cpml_v0", C.c_double), ("cpml_r", C.c_double),
         ("scale", C.c_double * 4),
         ("src_kind", C.c_int), ("src_ix", C.c_int), ("src_iy", C.c_int), ("src_iz", C.c_int),
-        ("src_factor", C.c_double), ("nthreads", C.c_int),
+        ("src_factor", C.c_double), ("nthreads", C.c_int), ("time_from_step", C.c_int),
     ]
 
 
@@ -42,6 +42,8 @@ def lib():
         _lib.orc_run.restype = C.c_int
         _lib.orc_ref_run.restype = C.c_int
         _lib.orc_ref_aux_name.restype = C.c_char_p
+        _lib.orc_last_step_seconds.restype = C.c_double
+        _lib.orc_threads.restype = C.c_int
     return _lib
 
 
@@ -116,7 +118,7 @@ def ricker(nt, dt, f0, t0=None, amp=1.0) -> np.ndarray:
 
 # ------------------------------------------------------------------------------ BEHF run
 def run(prob, precision: str = "f64", nthreads: int = 0, nt: int | None = None,
-        want_fields: bool = False):
+        want_fields: bool = False, time_from_step: int = 0):
     """Oracle run of a problem description (the attributes of behf.problems.Problem).
 
     Returns (seis [nrec, nt] float64, fields [13, nz, ny, nx] float64 or None)."""
@@ -132,6 +134,7 @@ def run(prob, precision: str = "f64", nthreads: int = 0, nt: int | None = None,
     cfg.src_kind = SOURCES[prob.src_kind]
     cfg.src_ix, cfg.src_iy, cfg.src_iz = prob.src
     cfg.nthreads = nthreads
+    cfg.time_from_step = time_from_step
     mod = _c(prob.mod, np.float32)
     w = _c(prob.wavelet[:nt], np.float32)
     ri = _c(prob.rec_ijk, np.int32).reshape(-1)
@@ -146,6 +149,15 @@ def run(prob, precision: str = "f64", nthreads: int = 0, nt: int | None = None,
     if rcode != 0:
         raise ValueError(f"orc_run failed with {rcode}")
     return seis, fo
+
+
+def last_step_seconds() -> float:
+    """Wall seconds of the time-step loop of the last run() (set-up excluded)."""
+    return float(lib().orc_last_step_seconds())
+
+
+def threads() -> int:
+    return int(lib().orc_threads())
 
 
 # ------------------------------------------------------------------------------ reference mode

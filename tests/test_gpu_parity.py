@@ -83,7 +83,14 @@ def test_source_kinds(behf_lib, oracle, kind):
     s, seis, _ = _run_gpu(prob, "f32")
     errs = _per_field_err(oracle, prob, seis, ref)
     assert np.abs(ref).max() > 0
-    assert max(errs.values()) < 1e-4, errs
+    tol = {2: 1e-4, 12: 1e-4}
+    if kind == "pressure":
+        # A pore-pressure injection drives vz only through the Darcy coupling: the vz trace is ~1e-4
+        # of the explosive source's, and FP32 storage alone (the oracle's own FP32 emulation) already
+        # puts it 1.5e-4 from FP64.  The injected field p keeps the 1e-4 bar.
+        tol[2] = 5e-4
+    for comp, e in errs.items():
+        assert e < tol[comp], (comp, errs)
     s.close()
 
 
@@ -154,7 +161,9 @@ def test_field_roundtrip_and_health(behf_lib):
     s.set_field("szz", v)
     np.testing.assert_array_equal(s.get_field("szz"), v)
     ok, norms = s.health()
-    assert ok and norms[behf.FIELD["szz"]] == pytest.approx(float(np.sum(v.astype(np.float64) ** 2)), rel=1e-12)
+    s_sigma = s.info()["scales"][2]  # health reports storage units: value * s_sigma for a stress
+    expect = float(np.sum((v.astype(np.float64) * s_sigma) ** 2))
+    assert ok and norms[behf.FIELD["szz"]] == pytest.approx(expect, rel=1e-12)
     v[3, 4, 5] = np.inf
     s.set_field("szz", v)
     ok, _ = s.health()
