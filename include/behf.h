@@ -177,6 +177,21 @@ behf_status behf_get_stream(behf_ctx* ctx, void** stream);
  * or ignores errors, kernel.cu:1926-1929). */
 behf_status behf_health(behf_ctx* ctx, double* norms);
 
+/* Energy norm and health flag of one field, without allocating any device memory.  No counterpart
+ * in the reference.  For callers that cannot allocate: a host application that owns all device
+ * memory through its own pool (nothing left for cudaMalloc), or a monitoring thread that checks a
+ * running simulation and must not stall the device with cudaFree.
+ *   field      device array of `precision` values laid out [nz][ny][pitch] with plane stride `plane`
+ *   norm_out   device double: sum of squares of the nx*ny*nz values (the storage units of the field)
+ *   flag_out   device int: 1 if any value is NaN/Inf or at the top of the storage range, else 0
+ *   stream     cudaStream_t to run on (NULL: the default stream); the call does not synchronize
+ * Fields up to 2^30 cells (1024^3); larger sizes are rejected with BEHF_ERR_INVALID.  Scratch is a
+ * fixed 512 KiB device array inside the library, held by every GPU that loads it until exit.  The
+ * first call on each device looks up that array's address: make it before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race. */
+behf_status behf_field_norm_noalloc(const void* field, int precision, int nx, int ny, int nz, long long pitch,
+                                    long long plane, double* norm_out, int* flag_out, void* stream);
+
 /* Text of the last error on this thread. */
 const char* behf_last_error(void);
 /* Library version string. */

@@ -112,6 +112,8 @@ def load() -> C.CDLL:
         "behf_update_wavelet": [C.c_void_p, C.c_int, P(C.c_float), C.c_int],
         "behf_get_seismograms_range": [C.c_void_p, C.c_int, C.c_int, P(C.c_double)],
         "behf_time_kernels": [C.c_void_p, C.c_int, P(C.c_double)],
+        "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
+                                    C.c_void_p, C.c_void_p, C.c_void_p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -280,6 +282,14 @@ class Solver:
         s = C.c_void_p()
         _check(self._lib.behf_get_stream(self._ctx, C.byref(s)))
         return s.value or 0
+
+
+def field_norm_noalloc(field_ptr: int, precision: str, nx: int, ny: int, nz: int, pitch: int, plane: int,
+                       norm_ptr: int, flag_ptr: int, stream: int = 0):
+    """behf_field_norm_noalloc on caller-owned device pointers (see include/behf.h): the energy norm and
+    health flag of one field without any device allocation.  Asynchronous on `stream`."""
+    _check(load().behf_field_norm_noalloc(C.c_void_p(field_ptr), PRECISION[precision], nx, ny, nz, pitch, plane,
+                                          C.c_void_p(norm_ptr), C.c_void_p(flag_ptr), C.c_void_p(stream)))
 
 
 def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:

@@ -65,6 +65,11 @@ double pow2_round(double s) { return std::ldexp(1.0, (int)std::lround(std::log2(
 
 }  // namespace
 
+namespace behf {
+// Error text for entry points defined in other translation units.
+void report_error(const char* msg) { g_err = msg; }
+}  // namespace behf
+
 struct behf_ctx {
     behf_grid grid{};
     int prec = BEHF_FP32;
