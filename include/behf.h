@@ -32,6 +32,7 @@ typedef int behf_status;
 #define BEHF_ERR_STATE (-4)     /* call out of order (e.g. run before the medium is set) */
 #define BEHF_ERR_NONFINITE (-5) /* the health check found a NaN/Inf or an overflow in a field */
 #define BEHF_ERR_UNSUPPORTED (-6)
+#define BEHF_ERR_TIMEOUT (-7)   /* a kernel's bounded pipeline wait gave up; results of that run are invalid */
 
 /* Storage precision of the wavefields (arithmetic is FP32 for the 16/32-bit kinds, FP64 for FP64). */
 typedef enum { BEHF_FP64 = 0, BEHF_FP32 = 1, BEHF_FP16 = 2, BEHF_BF16 = 3 } behf_precision;

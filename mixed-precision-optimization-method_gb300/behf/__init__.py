@@ -12,7 +12,8 @@ from pathlib import Path
 
 import numpy as np
 
-_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libbehf.so"
+# BEHF_LIBRARY overrides the in-tree build (e.g. to compare builds with different compile-time options).
+_LIB_PATH = Path(os.environ.get("BEHF_LIBRARY") or Path(__file__).resolve().parent / "_lib" / "libbehf.so")
 _lib = None
 
 FIELDS = ["vx", "vy", "vz", "qx", "qy", "qz", "sxx", "syy", "szz", "sxy", "sxz", "syz", "p"]

@@ -2,6 +2,7 @@
 // graph-captured time loop.  Replaces the reference's host/device boundary: main.cpp:1529-1743
 // (allocation and copies of the blockInfo arrays) and callCUDAKernel (kernel.cu:1728-2698).
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +12,7 @@
 #include "behf_aux.cuh"
 #include "behf_internal.cuh"
 #include "behf_medium.cuh"
+#include "kernels_tiled.cuh"
 
 using namespace behf;
 
@@ -114,9 +116,16 @@ struct behf_ctx {
     int* d_flag = nullptr;
     double* d_norm = nullptr;
     int nblk_health = 0;
+    // tiled kernels: TMA descriptors (built once, the arrays never move) and the device error word
+    bool tiled_ok = false;
+    tiled::VMaps* vmaps = nullptr;
+    tiled::TMaps* tmaps = nullptr;
+    int* d_err = nullptr;
 
     ~behf_ctx() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        std::free(vmaps);
+        std::free(tmaps);
         for (auto& a : allocs) cudaFree(a.first);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -156,9 +165,19 @@ namespace {
 
 template <class S>
 cudaError_t launch_update(behf_ctx* c, bool vel) {
-    const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && tiled_supported<S>(c->g);
-    if (tiled) return launch_tiled<S>(c->g, c->p, vel, c->stream);
+    const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok;
+    if (tiled)
+        return launch_tiled<S>(c->g, c->p, vel ? (const void*)c->vmaps : (const void*)c->tmaps, vel, c->stream);
     return launch_plain<S>(c->g, c->p, vel, c->stream);
+}
+
+template <class S>
+bool setup_tiled(behf_ctx* c) {
+    if (!tiled_supported<S>(c->g)) return false;
+    c->vmaps = static_cast<tiled::VMaps*>(std::aligned_alloc(64, (sizeof(tiled::VMaps) + 63) / 64 * 64));
+    c->tmaps = static_cast<tiled::TMaps*>(std::aligned_alloc(64, (sizeof(tiled::TMaps) + 63) / 64 * 64));
+    if (!c->vmaps || !c->tmaps) return false;
+    return tiled_build_maps<S>(c->g, c->p, c->vmaps, c->tmaps) == cudaSuccess;
 }
 
 cudaError_t dispatch_update(behf_ctx* c, bool vel) {
@@ -364,6 +383,8 @@ behf_status build_coefs(behf_ctx* c, const float* const mod[kNMod]) {
             c->g.kmulf[q] = 1.0f;
         }
     }
+    c->g.c_vw2 = (float)(sp * sq / (sv * ss));
+    c->g.c_s3 = (float)(ss * sv / (sp * sq));
     a.pass = 1;
     CK(aux_build_coefs<S>(a, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -500,6 +521,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     A((void**)&c->d_part, (size_t)c->nblk_health * 8);
     A((void**)&c->d_flag, sizeof(int));
     A((void**)&c->d_norm, kNField * 8);
+    A((void**)&c->d_err, sizeof(int));
     if (st) {
         delete c;
         return st;
@@ -509,8 +531,18 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
         g.kmuld[q] = 1.0;
         g.kmulf[q] = 1.0f;
     }
+    if (st == BEHF_OK && cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) st = BEHF_ERR_CUDA;
+    g.err = c->d_err;
     if (st == BEHF_OK) st = upload_profiles(c);
     if (st == BEHF_OK) st = zero_state(c);
+    if (st == BEHF_OK) {
+        switch (precision) {
+            case BEHF_FP32: c->tiled_ok = setup_tiled<float>(c); break;
+            case BEHF_FP16: c->tiled_ok = setup_tiled<__half>(c); break;
+            case BEHF_BF16: c->tiled_ok = setup_tiled<__nv_bfloat16>(c); break;
+            default: c->tiled_ok = false;
+        }
+    }
     if (st) {
         delete c;
         return st == BEHF_ERR_CUDA && g_err.empty() ? fail(st, "initialisation failed") : st;
@@ -691,6 +723,12 @@ behf_status behf_run_async(behf_ctx* c, int nsteps) {
 behf_status behf_sync(behf_ctx* c) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
     CK(cudaStreamSynchronize(c->stream));
+    int err = 0;
+    CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(c->d_err, 0, sizeof(int));
+        return fail(BEHF_ERR_TIMEOUT, "a tiled kernel's pipeline wait timed out; the step's results are invalid");
+    }
     return BEHF_OK;
 }
 
@@ -759,16 +797,8 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
     switch (opt) {
         case BEHF_OPT_KERNEL:
             if (value < BEHF_KERNEL_AUTO || value > BEHF_KERNEL_TILED) return fail(BEHF_ERR_INVALID, "bad kernel %d", value);
-            if (value == BEHF_KERNEL_TILED) {
-                bool ok = false;
-                switch (c->prec) {
-                    case BEHF_FP64: ok = tiled_supported<double>(c->g); break;
-                    case BEHF_FP32: ok = tiled_supported<float>(c->g); break;
-                    case BEHF_FP16: ok = tiled_supported<__half>(c->g); break;
-                    case BEHF_BF16: ok = tiled_supported<__nv_bfloat16>(c->g); break;
-                }
-                if (!ok) return fail(BEHF_ERR_UNSUPPORTED, "tiled kernel not available for this precision/radius/grid");
-            }
+            if (value == BEHF_KERNEL_TILED && !c->tiled_ok)
+                return fail(BEHF_ERR_UNSUPPORTED, "tiled kernel not available for this precision/radius/grid");
             c->kernel_opt = value;
             break;
         case BEHF_OPT_REF_BUG_COMPAT: c->g.bug = value ? 1 : 0; break;
@@ -793,14 +823,7 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
     double cpml = 0;
     for (int a = 0; a < 3; a++) cpml += c->g.W > 0 ? 16.0 * 2.0 * c->ws * c->g.W / n3[a] : 0.0;
     out->bytes_per_cell = 26.0 * c->es + 3.0 * c->ws + 20.0 * c->ks + cpml;
-    bool tiled = false;
-    switch (c->prec) {
-        case BEHF_FP64: tiled = tiled_supported<double>(c->g); break;
-        case BEHF_FP32: tiled = tiled_supported<float>(c->g); break;
-        case BEHF_FP16: tiled = tiled_supported<__half>(c->g); break;
-        case BEHF_BF16: tiled = tiled_supported<__nv_bfloat16>(c->g); break;
-    }
-    out->kernel = (c->kernel_opt != BEHF_KERNEL_PLAIN && tiled) ? BEHF_KERNEL_TILED : BEHF_KERNEL_PLAIN;
+    out->kernel = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? BEHF_KERNEL_TILED : BEHF_KERNEL_PLAIN;
     out->radius = c->g.R;
     out->precision = c->prec;
     out->launches = c->launches;

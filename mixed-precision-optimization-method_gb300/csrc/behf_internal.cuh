@@ -98,8 +98,13 @@ struct Geom {
     int R, L, W;           // stencil half-width, CPML width, slab width 2L+1 (0 without CPML)
     long long px, plane;   // row pitch and plane stride in elements
     int bug;               // reference vz/VW3y compatibility
+    int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out
     float kmulf[kNCoef];   // power-of-two multipliers of the stored coefficients
     double kmuld[kNCoef];
+    // Exact identities the tiled kernels use instead of reading two more arrays (effective, scaled values):
+    //   VW2 = VU2 * VW3 * c_vw2   (dt rho_f/rho / D = (rho_f/rho) (dt / D)),  c_vw2 = s_p s_q / (s_v s_sigma)
+    //   S3  = P1 * c_s3           (both C dt),                                 c_s3  = s_sigma s_v / (s_p s_q)
+    float c_vw2, c_s3;
 };
 
 __host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
@@ -108,7 +113,9 @@ __host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
 
 // Launchers (defined per translation unit).
 template <class S> cudaError_t launch_plain(const Geom& g, const DevPtrs& p, bool vel, cudaStream_t st);
-template <class S> cudaError_t launch_tiled(const Geom& g, const DevPtrs& p, bool vel, cudaStream_t st);
+// maps: the context's tiled::VMaps (vel) or tiled::TMaps (stress), host memory, 64-byte aligned.
+template <class S> cudaError_t launch_tiled(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st);
 template <class S> bool tiled_supported(const Geom& g);
+template <class S> cudaError_t tiled_build_maps(const Geom& g, const DevPtrs& p, void* vmaps, void* tmaps);
 
 }  // namespace behf

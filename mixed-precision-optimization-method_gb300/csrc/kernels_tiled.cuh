@@ -1,0 +1,214 @@
+// kernels_tiled.cuh -- z-marching velocity / stress kernels for sm_103a (FP16, BF16, FP32 storage).
+//
+// One CTA owns an xy tile of TXC x TY cells (64 x 8; 256 threads, each thread a pair of adjacent x cells,
+// one warp per tile row) and marches it through z, one plane per step:
+//   * the fields with a z-derivative live in a register queue of the 2R+1 planes around the current one,
+//     refilled by one coalesced load per step (the reference re-reads every neighbour from HBM,
+//     kernel.cu:172-185);
+//   * everything else for plane k -- the xy-halo boxes of the fields with x/y derivatives, the cell's own
+//     fields and its coefficients -- arrives by TMA (cp.async.bulk.tensor.3d) into a two-stage shared-
+//     memory ring, signalled by an mbarrier; the copies for plane k+1 are in flight while plane k is
+//     computed.  Halo boxes start on 16-byte x boundaries (x0 - 16 B) and TMA zero-fills outside the
+//     grid, which provides the ghost zeros of the domain faces;
+//   * x/y/z stencils are evaluated on cell pairs with packed FP32 arithmetic (fma.rn.f32x2);
+//   * CPML memory is touched only on slab cells (z: block-uniform, y: warp-uniform, x: per cell).
+// Every mbarrier wait is bounded: on timeout the CTA sets the context's error word, drains its
+// outstanding copies (bounded again) and exits, so the host sees BEHF_ERR_TIMEOUT instead of a hang.
+#pragma once
+#include <cuda.h>
+
+#include "behf_internal.cuh"
+
+namespace behf {
+namespace tiled {
+
+constexpr int TXC = 64;            // cells per tile row (x)
+constexpr int TY = 8;              // tile rows (y)
+constexpr int NTH = 32 * TY;       // threads per CTA
+constexpr long long kSpinLimit = 4000000000LL;  // clock64 cycles (~2 s) before a wait gives up
+
+template <class S> struct Pair;
+template <> struct Pair<__half> {
+    typedef __half2 T;
+    static __device__ __forceinline__ float2 f2(T v) { return __half22float2(v); }
+    static __device__ __forceinline__ T pack(float2 v) { return __float22half2_rn(v); }
+    static __device__ __forceinline__ __half one(float v) { return __float2half_rn(v); }
+};
+template <> struct Pair<__nv_bfloat16> {
+    typedef __nv_bfloat162 T;
+    static __device__ __forceinline__ float2 f2(T v) { return __bfloat1622float2(v); }
+    static __device__ __forceinline__ T pack(float2 v) { return __float22bfloat162_rn(v); }
+    static __device__ __forceinline__ __nv_bfloat16 one(float v) { return __float2bfloat16_rn(v); }
+};
+template <> struct Pair<float> {
+    typedef float2 T;
+    static __device__ __forceinline__ float2 f2(T v) { return v; }
+    static __device__ __forceinline__ T pack(float2 v) { return v; }
+    static __device__ __forceinline__ float one(float v) { return v; }
+};
+
+// Box geometry in elements.  X boxes carry an x halo of HX = 16 bytes each side, Y boxes a y halo of R
+// rows, XY boxes both; own-cell boxes are TXC x TY.
+template <class S, int R>
+struct Geo {
+    static constexpr int HX = 16 / (int)sizeof(S);
+    static constexpr int BW = TXC + 2 * HX;
+    static constexpr int BH = TY + 2 * R;
+    static constexpr int X_B = BW * TY * (int)sizeof(S);
+    static constexpr int Y_B = TXC * BH * (int)sizeof(S);
+    static constexpr int XY_B = BW * BH * (int)sizeof(S);
+    static constexpr int OWN_B = TXC * TY * (int)sizeof(S);
+    static constexpr int KOWN_B = TXC * TY * (int)sizeof(typename Traits<S>::K);
+    static constexpr int WOWN_B = TXC * TY * 4;  // FP32 Darcy factor
+};
+
+constexpr int al128(int b) { return (b + 127) & ~127; }
+
+// Stage layouts: see VOff / TOff in kernels_tiled_impl.cuh.  Velocity stage: halo boxes txx(X) tyy(Y)
+// txy(XY) txz(X) tyz(Y) p(XY), own vx vy vz qx qy qz, coefficients VW1x..z (FP32) then VW2x..z VW3x..z
+// VU1x..z VU2x..z.  Stress stage: halo vx vy vz (XY) qx (X) qy (Y), own sxx syy szz sxy sxz syz p,
+// coefficients P1 P2 S1 S2 S3 Sxy Sxz Syz.  Every region starts on a 128-byte boundary.
+struct VMaps {
+    CUtensorMap halo[6];  // txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY)
+    CUtensorMap own[6];   // vx vy vz qx qy qz
+    CUtensorMap coef[15]; // VW1x..z VW2x..z VW3x..z VU1x..z VU2x..z
+    CUtensorMap zlead[4]; // tzz txz tyz p, own-cell box at plane k+R
+};
+struct TMaps {
+    CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
+    CUtensorMap own[7];   // sxx syy szz sxy sxz syz p
+    CUtensorMap coef[8];  // P1 P2 S1 S2 S3 Sxy Sxz Syz
+    CUtensorMap zlead[4]; // vx vy vz qz, own-cell box at plane k+R
+};
+
+// ------------------------------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false after kSpinLimit cycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kSpinLimit) return false;
+    return true;
+}
+__device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+__device__ __forceinline__ void fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ------------------------------------------------------------------------------------- pair math
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+template <int R>
+__device__ __forceinline__ float wgt(int m) {
+    return (float)stencil_w<R>(m);
+}
+
+// Window of 2*RA+2 values around the pair (x, x+1), RA = R rounded up to even: w[d + RA] = f[x + d].
+template <class S, int R>
+struct XWin {
+    static constexpr int RA = (R + 1) & ~1;
+    float w[2 * RA + 2];
+    __device__ __forceinline__ void load(const S* rowp) {  // rowp points at f[x] in smem (x even)
+        typedef typename Pair<S>::T P;
+#pragma unroll
+        for (int u = 0; u <= RA; u++) {
+            const float2 v = Pair<S>::f2(*reinterpret_cast<const P*>(rowp - RA + 2 * u));
+            w[2 * u] = v.x;
+            w[2 * u + 1] = v.y;
+        }
+    }
+    // forward (at x+1/2): sum_m c_m (f[x+m] - f[x-m+1]) for both cells
+    __device__ __forceinline__ float2 fwd() const {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int m = 1; m <= R; m++) {
+            const float c = wgt<R>(m);
+            acc = fma2(f2(c, c), f2(w[RA + m], w[RA + m + 1]), acc);
+            acc = fma2(f2(-c, -c), f2(w[RA - m + 1], w[RA - m + 2]), acc);
+        }
+        return acc;
+    }
+    // backward (at x): sum_m c_m (f[x+m-1] - f[x-m])
+    __device__ __forceinline__ float2 bwd() const {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int m = 1; m <= R; m++) {
+            const float c = wgt<R>(m);
+            acc = fma2(f2(c, c), f2(w[RA + m - 1], w[RA + m]), acc);
+            acc = fma2(f2(-c, -c), f2(w[RA - m], w[RA - m + 1]), acc);
+        }
+        return acc;
+    }
+};
+
+// Column of 2R+1 pairs: v[R + d] = pair at offset d (rows in y, or planes in z).
+template <int R>
+__device__ __forceinline__ float2 col_fwd(const float2* v) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int m = 1; m <= R; m++) {
+        const float c = wgt<R>(m);
+        acc = fma2(f2(c, c), v[R + m], acc);
+        acc = fma2(f2(-c, -c), v[R - m + 1], acc);
+    }
+    return acc;
+}
+template <int R>
+__device__ __forceinline__ float2 col_bwd(const float2* v) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int m = 1; m <= R; m++) {
+        const float c = wgt<R>(m);
+        acc = fma2(f2(c, c), v[R + m - 1], acc);
+        acc = fma2(f2(-c, -c), v[R - m], acc);
+    }
+    return acc;
+}
+
+template <class S, int R>
+__device__ __forceinline__ void load_col(float2* v, const S* p, int stride) {  // p at row/plane 0 of the pair
+    typedef typename Pair<S>::T P;
+#pragma unroll
+    for (int d = -R; d <= R; d++) v[R + d] = Pair<S>::f2(*reinterpret_cast<const P*>(p + d * stride));
+}
+
+// Trapezoidal CPML memory update of one cell: psi = A psi + B (A prev + D); prev = D; returns D + psi.
+__device__ __forceinline__ float pml1(float D, float* psi, float* prv, float A, float B) {
+    const float pn = A * (*psi) + B * (A * (*prv) + D);
+    *psi = pn;
+    *prv = D;
+    return D + pn;
+}
+
+}  // namespace tiled
+}  // namespace behf

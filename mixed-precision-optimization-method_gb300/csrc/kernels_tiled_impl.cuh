@@ -1,0 +1,658 @@
+// kernels_tiled_impl.cuh -- bodies of the z-marching kernels (included once per storage precision by
+// kernels_tiled_{f16,bf16,f32}.cu so the three instantiations compile in parallel).
+#pragma once
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "kernels_tiled.cuh"
+
+namespace behf {
+namespace tiled {
+
+// Pipeline depth: stages in the shared-memory ring (NS - 1 planes in flight while one is computed).
+template <class S> struct Depth {
+    static constexpr int NS = sizeof(S) == 2 ? 3 : 2;
+    static constexpr int MINB = sizeof(S) == 2 ? 2 : 1;  // CTAs per SM the launch bounds aim for
+};
+
+// Byte offsets inside one stage.  Velocity: halo txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY), own
+// vx vy vz qx qy qz, VW1x..z (FP32), VW3x..z VU1x..z VU2x..z (VW2 = VU2 VW3 c_vw2 is derived), then the
+// z-queue fields at plane k+R (the queue's leading plane).
+template <class S, int R>
+struct VOff {
+    typedef Geo<S, R> G;
+    static constexpr int X = al128(G::X_B), Y = al128(G::Y_B), XY = al128(G::XY_B);
+    __host__ __device__ static constexpr int halo(int i) {
+        return i == 0 ? 0 : i == 1 ? X : i == 2 ? X + Y : i == 3 ? X + Y + XY : i == 4 ? 2 * X + Y + XY : 2 * X + 2 * Y + XY;
+    }
+    static constexpr int own = 2 * X + 2 * Y + 2 * XY;
+    static constexpr int wof = own + 6 * al128(G::OWN_B);
+    static constexpr int kof = wof + 3 * al128(G::WOWN_B);
+    static constexpr int NK = 9;
+    static constexpr int zof = kof + NK * al128(G::KOWN_B);  // z-queue leading plane k+R: tzz txz tyz p
+    static constexpr int stage = zof + 4 * al128(G::OWN_B);
+    static constexpr uint32_t bytes =
+        2 * (G::X_B + G::Y_B + G::XY_B) + 10 * G::OWN_B + 3 * G::WOWN_B + NK * G::KOWN_B;
+};
+// Stress: halo vx vy vz (XY) qx (X) qy (Y), own sxx syy szz sxy sxz syz p, P1 P2 S1 S2 Sxy Sxz Syz.
+// (S3 = P1 c_s3 is derived.)
+template <class S, int R>
+struct TOff {
+    typedef Geo<S, R> G;
+    static constexpr int X = al128(G::X_B), Y = al128(G::Y_B), XY = al128(G::XY_B);
+    __host__ __device__ static constexpr int halo(int i) { return i < 3 ? i * XY : i == 3 ? 3 * XY : 3 * XY + X; }
+    static constexpr int own = 3 * XY + X + Y;
+    static constexpr int kof = own + 7 * al128(G::OWN_B);
+    static constexpr int NK = 7;
+    static constexpr int zof = kof + NK * al128(G::KOWN_B);  // z-queue leading plane k+R: vx vy vz qz
+    static constexpr int stage = zof + 4 * al128(G::OWN_B);
+    static constexpr uint32_t bytes = 3 * G::XY_B + G::X_B + G::Y_B + 11 * G::OWN_B + NK * G::KOWN_B;
+};
+
+__device__ __forceinline__ float comp(float2 v, int c) { return c ? v.y : v.x; }
+__device__ __forceinline__ void setc(float2& v, int c, float x) {
+    if (c) v.y = x;
+    else v.x = x;
+}
+__device__ __forceinline__ float prof(const void* a, int i) { return reinterpret_cast<const float*>(a)[i]; }
+
+// CPML of the four derivatives of one axis for one cell: all eight loads first, then the updates, then the
+// eight stores (the arrays cannot alias, but the compiler cannot know; batching keeps one memory latency).
+__device__ __forceinline__ void pml4(const DevPtrs& p, int ax, int slot0, long long so, float A, float B, float A2,
+                                     float B2, float& d0, float& d1, float& d2, float& d3, bool half0, bool half1,
+                                     bool half2, bool half3) {
+    float* ps[4];
+    float* pv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        ps[j] = reinterpret_cast<float*>(p.psi[ax][slot0 + j]) + so;
+        pv[j] = reinterpret_cast<float*>(p.prv[ax][slot0 + j]) + so;
+    }
+    float s[4], v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        s[j] = *ps[j];
+        v[j] = *pv[j];
+    }
+    float* d[4] = {&d0, &d1, &d2, &d3};
+    const bool h[4] = {half0, half1, half2, half3};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float a = h[j] ? A2 : A, b = h[j] ? B2 : B;
+        const float D = *d[j];
+        const float pn = a * s[j] + b * (a * v[j] + D);  // psi = A psi + B (A prev + D)
+        s[j] = pn;
+        v[j] = D;
+        *d[j] = D + pn;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        *ps[j] = s[j];
+        *pv[j] = v[j];
+    }
+}
+
+// CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
+// velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.
+template <int SLOT0>
+__device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x, int y, int k, bool a0, bool a1,
+                                         float2& dx0, float2& dx1, float2& dx2, float2& dx3, const bool hx[4],
+                                         float2& dy0, float2& dy1, float2& dy2, float2& dy3, const bool hy[4],
+                                         float2& dz0, float2& dz1, float2& dz2, float2& dz3, const bool hz[4]) {
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const int xc = x + c;
+        const int si = (c ? a1 : a0) ? slab_index(xc, g.nx, g.L) : -1;
+        if (si >= 0) {
+            const long long so = ((long long)k * g.ny + y) * g.W + si;
+            float a = comp(dx0, c), b = comp(dx1, c), d = comp(dx2, c), e = comp(dx3, c);
+            pml4(p, 0, SLOT0, so, prof(p.pa[0], xc), prof(p.pb[0], xc), prof(p.pa2[0], xc), prof(p.pb2[0], xc), a, b,
+                 d, e, hx[0], hx[1], hx[2], hx[3]);
+            setc(dx0, c, a);
+            setc(dx1, c, b);
+            setc(dx2, c, d);
+            setc(dx3, c, e);
+        }
+    }
+    const int sj = slab_index(y, g.ny, g.L);
+    if (sj >= 0) {
+        const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            if (!(c ? a1 : a0)) continue;
+            const long long so = ((long long)k * g.W + sj) * g.nx + x + c;
+            float a = comp(dy0, c), b = comp(dy1, c), d = comp(dy2, c), e = comp(dy3, c);
+            pml4(p, 1, SLOT0, so, A, B, A2, B2, a, b, d, e, hy[0], hy[1], hy[2], hy[3]);
+            setc(dy0, c, a);
+            setc(dy1, c, b);
+            setc(dy2, c, d);
+            setc(dy3, c, e);
+        }
+    }
+    const int sk = slab_index(k, g.nz, g.L);
+    if (sk >= 0) {
+        const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            if (!(c ? a1 : a0)) continue;
+            const long long so = ((long long)sk * g.ny + y) * g.nx + x + c;
+            float a = comp(dz0, c), b = comp(dz1, c), d = comp(dz2, c), e = comp(dz3, c);
+            pml4(p, 2, SLOT0, so, A, B, A2, B2, a, b, d, e, hz[0], hz[1], hz[2], hz[3]);
+            setc(dz0, c, a);
+            setc(dz1, c, b);
+            setc(dz2, c, d);
+            setc(dz3, c, e);
+        }
+    }
+}
+
+// Store a pair, or the one active cell of it.
+template <class S>
+__device__ __forceinline__ void store_pair(S* dst, typename Pair<S>::T v, bool a0, bool a1) {
+    if (a0 && a1) {
+        *reinterpret_cast<typename Pair<S>::T*>(dst) = v;
+    } else {
+        const float2 f = Pair<S>::f2(v);
+        if (a0) dst[0] = Pair<S>::one(f.x);
+        if (a1) dst[1] = Pair<S>::one(f.y);
+    }
+}
+
+// mbarrier ring of NS stages: phase bit s is the parity of stage s's next completion.
+template <int NS>
+struct Ring {
+    uint64_t* bar;
+    uint32_t phase;
+    __device__ __forceinline__ bool wait(int st) { return mbar_wait(&bar[st], (phase >> st) & 1u); }
+    __device__ __forceinline__ void advance(int st) { phase ^= 1u << st; }
+    // drain every stage with copies in flight (issued for planes k .. k+NS-2), each wait bounded
+    __device__ __forceinline__ void drain(int it, int k, int ke) {
+        for (int j = 0; j < NS - 1 && k + j < ke; j++) {
+            const int st = (it + j) % NS;
+            mbar_wait(&bar[st], (phase >> st) & 1u);
+            phase ^= 1u << st;
+        }
+    }
+};
+
+// ----------------------------------------------------------------------------------------- velocity
+template <class S, int R>
+__global__ void __launch_bounds__(NTH, Depth<S>::MINB)
+    k_vel(const __grid_constant__ VMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
+    typedef Pair<S> PS;
+    typedef typename PS::T P;
+    typedef typename Traits<S>::K K;
+    typedef typename Pair<K>::T KP;
+    typedef Geo<S, R> G;
+    typedef VOff<S, R> O;
+    constexpr int NS = Depth<S>::NS;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar[NS];
+    // TMA destinations start on 128-byte boundaries: round the dynamic base up (128 B are reserved for it)
+    unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int x0 = blockIdx.x * TXC, y0 = blockIdx.y * TY;
+    const int kb = R + blockIdx.z * zchunk;
+    const int ke = min(kb + zchunk, g.nz - R);
+    if (kb >= ke) return;
+    const int xl = 2 * tx, x = x0 + xl, y = y0 + ty;
+    const bool a0 = x >= R && x < g.nx - R, a1 = x + 1 >= R && x + 1 < g.nx - R;
+    const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
+    const long long col = (long long)y * g.px + x;
+
+    if (tid == 0) {
+        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int st, int k) {
+        unsigned char* b = smem + st * O::stage;
+        uint64_t* br = &bar[st];
+        mbar_expect_tx(br, O::bytes);
+        tma3(b + O::halo(0), &maps.halo[0], br, x0 - G::HX, y0, k);      // txx  (x halo)
+        tma3(b + O::halo(1), &maps.halo[1], br, x0, y0 - R, k);          // tyy  (y halo)
+        tma3(b + O::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // txy  (x, y halo)
+        tma3(b + O::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // txz  (x halo)
+        tma3(b + O::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // tyz  (y halo)
+        tma3(b + O::halo(5), &maps.halo[5], br, x0 - G::HX, y0 - R, k);  // p    (x, y halo)
+#pragma unroll
+        for (int q = 0; q < 6; q++) tma3(b + O::own + q * al128(G::OWN_B), &maps.own[q], br, x0, y0, k);
+#pragma unroll
+        for (int q = 0; q < 3; q++) tma3(b + O::wof + q * al128(G::WOWN_B), &maps.coef[q], br, x0, y0, k);
+#pragma unroll
+        for (int q = 0; q < O::NK; q++)  // VW3x..z VU1x..z VU2x..z
+            tma3(b + O::kof + q * al128(G::KOWN_B), &maps.coef[6 + q], br, x0, y0, k);
+#pragma unroll
+        for (int q = 0; q < 4; q++) tma3(b + O::zof + q * al128(G::OWN_B), &maps.zlead[q], br, x0, y0, k + R);
+    };
+
+    // z queues: tzz (forward), txz (backward), tyz (backward), p (forward).  Q[f][d] = plane k-R+d for
+    // d < 2R in registers; plane k+R (d = 2R) comes with the stage.
+    const S* qsrc[4] = {reinterpret_cast<const S*>(p.f[BEHF_SZZ]), reinterpret_cast<const S*>(p.f[BEHF_SXZ]),
+                        reinterpret_cast<const S*>(p.f[BEHF_SYZ]), reinterpret_cast<const S*>(p.f[BEHF_P])};
+    P Q[4][2 * R];
+    if (live) {
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+#pragma unroll
+            for (int d = 0; d < 2 * R; d++)
+                Q[f][d] = *reinterpret_cast<const P*>(qsrc[f] + (long long)(kb - R + d) * g.plane + col);
+    }
+    if (tid == 0)
+        for (int j = 0; j < NS - 1 && kb + j < ke; j++) issue(j, kb + j);
+    Ring<NS> ring{bar, 0u};
+    for (int k = kb, it = 0; k < ke; k++, it++) {
+        const int st = it % NS;
+        const bool ok = ring.wait(st);
+        if (__syncthreads_or(!ok)) {
+            if (!ok) atomicExch(g.err, 1);
+            if (tid == 0) ring.drain(it, k, ke);
+            return;
+        }
+        ring.advance(st);
+        if (tid == 0 && k + NS - 1 < ke) {
+            fence_async();
+            issue((it + NS - 1) % NS, k + NS - 1);
+        }
+        const unsigned char* b = smem + st * O::stage;
+        const int oe = ty * TXC + xl;  // element offset of the pair in an own-cell box
+        if (live) {
+            const S* txx = reinterpret_cast<const S*>(b + O::halo(0));
+            const S* tyy = reinterpret_cast<const S*>(b + O::halo(1));
+            const S* txy = reinterpret_cast<const S*>(b + O::halo(2));
+            const S* txz = reinterpret_cast<const S*>(b + O::halo(3));
+            const S* tyz = reinterpret_cast<const S*>(b + O::halo(4));
+            const S* pp = reinterpret_cast<const S*>(b + O::halo(5));
+            const int rX = ty * G::BW + G::HX + xl;          // X box: row ty
+            const int rXY = (ty + R) * G::BW + G::HX + xl;   // XY box: row ty + R
+            const int rY = (ty + R) * TXC + xl;              // Y box: row ty + R
+            XWin<S, R> w;
+            w.load(txx + rX);
+            float2 x1 = w.fwd();
+            w.load(pp + rXY);
+            float2 s1 = w.fwd();
+            w.load(txy + rXY);
+            float2 y2 = w.bwd();
+            w.load(txz + rX);
+            float2 z2 = w.bwd();
+            float2 cv[2 * R + 1];
+            load_col<S, R>(cv, tyy + rY, TXC);
+            float2 y1 = col_fwd<R>(cv);
+            load_col<S, R>(cv, pp + rXY, G::BW);
+            float2 s2 = col_fwd<R>(cv);
+            load_col<S, R>(cv, txy + rXY, G::BW);
+            float2 x2 = col_bwd<R>(cv);
+            load_col<S, R>(cv, tyz + rY, TXC);
+            float2 z3 = col_bwd<R>(cv);
+            auto zcol = [&](int f) {
+#pragma unroll
+                for (int d = 0; d < 2 * R; d++) cv[d] = PS::f2(Q[f][d]);
+                cv[2 * R] = PS::f2(*reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S)));
+            };
+            zcol(0);
+            float2 z1 = col_fwd<R>(cv);
+            zcol(3);
+            float2 s3 = col_fwd<R>(cv);
+            zcol(1);
+            float2 x3 = col_bwd<R>(cv);
+            zcol(2);
+            float2 y3 = col_bwd<R>(cv);
+
+            if (g.W > 0) {
+                // x: x1 (fwd), s1 (fwd), y2 (bwd), z2 (bwd); y: y1, s2 (fwd), x2, z3 (bwd);
+                // z: z1, s3 (fwd), x3, y3 (bwd)
+                const bool hf[4] = {true, true, false, false};
+                pml_pair<0>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
+            }
+            const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
+            const float2 dp[3] = {s1, s2, s3};
+            auto kc = [&](int q, int j) {  // stage slot q, multiplier of coefficient j
+                const KP kv = *reinterpret_cast<const KP*>(b + O::kof + q * al128(G::KOWN_B) + oe * sizeof(K));
+                return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j]));
+            };
+            const long long go = (long long)k * g.plane + col;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const P qo_s = *reinterpret_cast<const P*>(b + O::own + (3 + a) * al128(G::OWN_B) + oe * sizeof(S));
+                const P vo_s = *reinterpret_cast<const P*>(b + O::own + a * al128(G::OWN_B) + oe * sizeof(S));
+                const float2 vw1 = *reinterpret_cast<const float2*>(b + O::wof + a * al128(G::WOWN_B) + oe * 4);
+                const float2 vw3 = kc(a, VW3X + a);
+                const float2 vu1 = kc(3 + a, VU1X + a), vu2 = kc(6 + a, VU2X + a);
+                const float2 vw2 = mul2(mul2(vu2, vw3), f2(g.c_vw2, g.c_vw2));
+                const float2 vw3p = (a == 2 && g.bug) ? kc(1, VW3Y) : vw3;  // reference: vz uses VW3y
+                const float2 qo = PS::f2(qo_s);
+                // q' = VW1 q - VW2 sum(d sigma) - VW3 d p
+                const float2 t = fma2(vw2, sum[a], mul2(vw3p, dp[a]));
+                const float2 qn = fma2(vw1, qo, make_float2(-t.x, -t.y));
+                const P qs = PS::pack(qn);
+                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_QX + a]) + go, qs, a0, a1);
+                // v' = v + VU1 sum(d sigma) - VU2 (q' - q)
+                const float2 dq = sub2(PS::f2(qs), qo);
+                const float2 vn = fma2(vu1, sum[a], fma2(make_float2(-vu2.x, -vu2.y), dq, PS::f2(vo_s)));
+                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, PS::pack(vn), a0, a1);
+            }
+        }
+        if (live && k + 1 < ke) {
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+#pragma unroll
+                for (int d = 0; d < 2 * R - 1; d++) Q[f][d] = Q[f][d + 1];
+                Q[f][2 * R - 1] = *reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S));
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------- stress
+template <class S, int R>
+__global__ void __launch_bounds__(NTH, Depth<S>::MINB)
+    k_str(const __grid_constant__ TMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
+    typedef Pair<S> PS;
+    typedef typename PS::T P;
+    typedef typename Traits<S>::K K;
+    typedef typename Pair<K>::T KP;
+    typedef Geo<S, R> G;
+    typedef TOff<S, R> O;
+    constexpr int NS = Depth<S>::NS;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar[NS];
+    unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int x0 = blockIdx.x * TXC, y0 = blockIdx.y * TY;
+    const int kb = R + blockIdx.z * zchunk;
+    const int ke = min(kb + zchunk, g.nz - R);
+    if (kb >= ke) return;
+    const int xl = 2 * tx, x = x0 + xl, y = y0 + ty;
+    const bool a0 = x >= R && x < g.nx - R, a1 = x + 1 >= R && x + 1 < g.nx - R;
+    const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
+    const long long col = (long long)y * g.px + x;
+
+    if (tid == 0) {
+        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        fence_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int st, int k) {
+        unsigned char* b = smem + st * O::stage;
+        uint64_t* br = &bar[st];
+        mbar_expect_tx(br, O::bytes);
+        tma3(b + O::halo(0), &maps.halo[0], br, x0 - G::HX, y0 - R, k);  // vx (x, y halo)
+        tma3(b + O::halo(1), &maps.halo[1], br, x0 - G::HX, y0 - R, k);  // vy
+        tma3(b + O::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
+        tma3(b + O::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // qx (x halo)
+        tma3(b + O::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // qy (y halo)
+#pragma unroll
+        for (int q = 0; q < 7; q++) tma3(b + O::own + q * al128(G::OWN_B), &maps.own[q], br, x0, y0, k);
+#pragma unroll
+        for (int q = 0; q < O::NK; q++) {  // P1 P2 S1 S2 Sxy Sxz Syz (map order P1 P2 S1 S2 S3 Sxy Sxz Syz)
+            const int m = q < 4 ? q : q + 1;
+            tma3(b + O::kof + q * al128(G::KOWN_B), &maps.coef[m], br, x0, y0, k);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) tma3(b + O::zof + q * al128(G::OWN_B), &maps.zlead[q], br, x0, y0, k + R);
+    };
+
+    // z queues: vx (forward), vy (forward), vz (backward), qz (backward); registers hold planes k-R..k+R-1,
+    // the stage holds plane k+R.
+    const S* qsrc[4] = {reinterpret_cast<const S*>(p.f[BEHF_VX]), reinterpret_cast<const S*>(p.f[BEHF_VY]),
+                        reinterpret_cast<const S*>(p.f[BEHF_VZ]), reinterpret_cast<const S*>(p.f[BEHF_QZ])};
+    P Q[4][2 * R];
+    if (live) {
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+#pragma unroll
+            for (int d = 0; d < 2 * R; d++)
+                Q[f][d] = *reinterpret_cast<const P*>(qsrc[f] + (long long)(kb - R + d) * g.plane + col);
+    }
+    if (tid == 0)
+        for (int j = 0; j < NS - 1 && kb + j < ke; j++) issue(j, kb + j);
+    Ring<NS> ring{bar, 0u};
+    for (int k = kb, it = 0; k < ke; k++, it++) {
+        const int st = it % NS;
+        const bool ok = ring.wait(st);
+        if (__syncthreads_or(!ok)) {
+            if (!ok) atomicExch(g.err, 1);
+            if (tid == 0) ring.drain(it, k, ke);
+            return;
+        }
+        ring.advance(st);
+        if (tid == 0 && k + NS - 1 < ke) {
+            fence_async();
+            issue((it + NS - 1) % NS, k + NS - 1);
+        }
+        const unsigned char* b = smem + st * O::stage;
+        const int oe = ty * TXC + xl;
+        if (live) {
+            const S* vx = reinterpret_cast<const S*>(b + O::halo(0));
+            const S* vy = reinterpret_cast<const S*>(b + O::halo(1));
+            const S* vz = reinterpret_cast<const S*>(b + O::halo(2));
+            const S* qx = reinterpret_cast<const S*>(b + O::halo(3));
+            const S* qy = reinterpret_cast<const S*>(b + O::halo(4));
+            const int rX = ty * G::BW + G::HX + xl;
+            const int rXY = (ty + R) * G::BW + G::HX + xl;
+            const int rY = (ty + R) * TXC + xl;
+            XWin<S, R> w;
+            w.load(vx + rXY);
+            float2 uxx = w.bwd();
+            w.load(vy + rXY);
+            float2 uyx = w.fwd();
+            w.load(vz + rXY);
+            float2 uzx = w.fwd();
+            w.load(qx + rX);
+            float2 wx = w.bwd();
+            float2 cv[2 * R + 1];
+            load_col<S, R>(cv, vy + rXY, G::BW);
+            float2 uyy = col_bwd<R>(cv);
+            load_col<S, R>(cv, vx + rXY, G::BW);
+            float2 uxy = col_fwd<R>(cv);
+            load_col<S, R>(cv, vz + rXY, G::BW);
+            float2 uzy = col_fwd<R>(cv);
+            load_col<S, R>(cv, qy + rY, TXC);
+            float2 wy = col_bwd<R>(cv);
+            auto zcol = [&](int f) {
+#pragma unroll
+                for (int d = 0; d < 2 * R; d++) cv[d] = PS::f2(Q[f][d]);
+                cv[2 * R] = PS::f2(*reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S)));
+            };
+            zcol(2);
+            float2 uzz = col_bwd<R>(cv);
+            zcol(3);
+            float2 wz = col_bwd<R>(cv);
+            zcol(0);
+            float2 uxz = col_fwd<R>(cv);
+            zcol(1);
+            float2 uyz = col_fwd<R>(cv);
+
+            if (g.W > 0) {
+                // x: uxx, wx (bwd), uyx, uzx (fwd); y: uyy, wy (bwd), uxy, uzy (fwd); z: uzz, wz (bwd), uxz, uyz (fwd)
+                const bool hf[4] = {false, false, true, true};
+                pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
+            }
+            const float2 dv = add2(add2(uxx, uyy), uzz);
+            const float2 dq = add2(add2(wx, wy), wz);
+            auto kc = [&](int q, int j) {
+                const KP kv = *reinterpret_cast<const KP*>(b + O::kof + q * al128(G::KOWN_B) + oe * sizeof(K));
+                return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j]));
+            };
+            auto own = [&](int q) {
+                return PS::f2(*reinterpret_cast<const P*>(b + O::own + q * al128(G::OWN_B) + oe * sizeof(S)));
+            };
+            const long long go = (long long)k * g.plane + col;
+            auto put = [&](int field, float2 v) {
+                store_pair<S>(reinterpret_cast<S*>(p.f[field]) + go, PS::pack(v), a0, a1);
+            };
+            const float2 p1 = kc(0, P1), p2 = kc(1, P2), g1 = kc(2, S1), g2 = kc(3, S2);
+            const float2 g3dq = mul2(mul2(p1, f2(g.c_s3, g.c_s3)), dq);  // S3 = P1 c_s3
+            // p' = p - P1 div v - P2 div q
+            put(BEHF_P, sub2(own(6), fma2(p1, dv, mul2(p2, dq))));
+            // s_ii' = s_ii + S1 (d_jj + d_kk) + S2 d_ii + S3 div q
+            put(BEHF_SXX, add2(own(0), fma2(g1, add2(uyy, uzz), fma2(g2, uxx, g3dq))));
+            put(BEHF_SYY, add2(own(1), fma2(g1, add2(uxx, uzz), fma2(g2, uyy, g3dq))));
+            put(BEHF_SZZ, add2(own(2), fma2(g1, add2(uxx, uyy), fma2(g2, uzz, g3dq))));
+            // s_ij' = s_ij + S_ij (d_j v_i + d_i v_j)
+            put(BEHF_SXY, fma2(kc(4, SXYC), add2(uxy, uyx), own(3)));
+            put(BEHF_SXZ, fma2(kc(5, SXZC), add2(uxz, uzx), own(4)));
+            put(BEHF_SYZ, fma2(kc(6, SYZC), add2(uyz, uzy), own(5)));
+        }
+        if (live && k + 1 < ke) {
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+#pragma unroll
+                for (int d = 0; d < 2 * R - 1; d++) Q[f][d] = Q[f][d + 1];
+                Q[f][2 * R - 1] = *reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S));
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------- host side
+inline PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    return fn;
+}
+
+template <class T> inline CUtensorMapDataType dtype_of();
+template <> inline CUtensorMapDataType dtype_of<__half>() { return CU_TENSOR_MAP_DATA_TYPE_FLOAT16; }
+template <> inline CUtensorMapDataType dtype_of<__nv_bfloat16>() { return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16; }
+template <> inline CUtensorMapDataType dtype_of<float>() { return CU_TENSOR_MAP_DATA_TYPE_FLOAT32; }
+
+// 3-D map over a pitched [nz][ny][px] array of T (logical extent nx), box bw x bh x 1.
+template <class T>
+inline bool encode(CUtensorMap* m, const Geom& g, void* base, int bw, int bh) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)(g.px * sizeof(T)), (cuuint64_t)(g.plane * sizeof(T))};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, dtype_of<T>(), 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <class S, int R>
+bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
+    typedef Geo<S, R> G;
+    typedef typename Traits<S>::K K;
+    bool ok = true;
+    // velocity
+    ok &= encode<S>(&vm->halo[0], g, p.f[BEHF_SXX], G::BW, TY);
+    ok &= encode<S>(&vm->halo[1], g, p.f[BEHF_SYY], TXC, G::BH);
+    ok &= encode<S>(&vm->halo[2], g, p.f[BEHF_SXY], G::BW, G::BH);
+    ok &= encode<S>(&vm->halo[3], g, p.f[BEHF_SXZ], G::BW, TY);
+    ok &= encode<S>(&vm->halo[4], g, p.f[BEHF_SYZ], TXC, G::BH);
+    ok &= encode<S>(&vm->halo[5], g, p.f[BEHF_P], G::BW, G::BH);
+    for (int q = 0; q < 6; q++) ok &= encode<S>(&vm->own[q], g, p.f[BEHF_VX + q], TXC, TY);
+    for (int q = 0; q < 3; q++) ok &= encode<float>(&vm->coef[q], g, p.k[q], TXC, TY);
+    for (int q = 3; q < 15; q++) ok &= encode<K>(&vm->coef[q], g, p.k[q], TXC, TY);
+    ok &= encode<S>(&vm->zlead[0], g, p.f[BEHF_SZZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[1], g, p.f[BEHF_SXZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[2], g, p.f[BEHF_SYZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[3], g, p.f[BEHF_P], TXC, TY);
+    // stress
+    ok &= encode<S>(&tm->halo[0], g, p.f[BEHF_VX], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[1], g, p.f[BEHF_VY], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[2], g, p.f[BEHF_VZ], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[3], g, p.f[BEHF_QX], G::BW, TY);
+    ok &= encode<S>(&tm->halo[4], g, p.f[BEHF_QY], TXC, G::BH);
+    for (int q = 0; q < 7; q++) ok &= encode<S>(&tm->own[q], g, p.f[BEHF_SXX + q], TXC, TY);
+    for (int q = 0; q < 8; q++) ok &= encode<K>(&tm->coef[q], g, p.k[P1 + q], TXC, TY);
+    ok &= encode<S>(&tm->zlead[0], g, p.f[BEHF_VX], TXC, TY);
+    ok &= encode<S>(&tm->zlead[1], g, p.f[BEHF_VY], TXC, TY);
+    ok &= encode<S>(&tm->zlead[2], g, p.f[BEHF_VZ], TXC, TY);
+    ok &= encode<S>(&tm->zlead[3], g, p.f[BEHF_QZ], TXC, TY);
+    return ok;
+}
+
+inline int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
+template <class S, int R>
+cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) {
+    constexpr int NS = Depth<S>::NS;
+    const int nbx = (g.nx - R + TXC - 1) / TXC, nby = (g.ny - R + TY - 1) / TY;
+    const int planes = g.nz - 2 * R;
+    // enough CTAs for every SM: split z into chunks when the xy tiling alone is too small
+    const int target = 2 * Depth<S>::MINB * num_sms();
+    int nzc = (target + nbx * nby - 1) / (nbx * nby);
+    nzc = nzc < 1 ? 1 : nzc;
+    const int maxc = planes / 16 > 1 ? planes / 16 : 1;
+    nzc = nzc > maxc ? maxc : nzc;
+    const int zchunk = (planes + nzc - 1) / nzc;
+    const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
+    if (vel) {
+        const int smem = NS * VOff<S, R>::stage + 128;
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_vel<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        k_vel<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const VMaps*>(maps), g, p, zchunk);
+    } else {
+        const int smem = NS * TOff<S, R>::stage + 128;
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(k_str<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        k_str<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const TMaps*>(maps), g, p, zchunk);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace tiled
+
+#define BEHF_TILED_INSTANTIATE(S)                                                                           \
+    template <>                                                                                            \
+    bool tiled_supported<S>(const Geom& g) {                                                               \
+        return g.R >= 1 && g.R <= 4 && tiled::encoder() != nullptr && g.nz > 2 * g.R;                      \
+    }                                                                                                      \
+    template <>                                                                                            \
+    cudaError_t tiled_build_maps<S>(const Geom& g, const DevPtrs& p, void* vm, void* tm) {                 \
+        bool ok = false;                                                                                   \
+        auto* v = reinterpret_cast<tiled::VMaps*>(vm);                                                     \
+        auto* t = reinterpret_cast<tiled::TMaps*>(tm);                                                     \
+        switch (g.R) {                                                                                     \
+            case 1: ok = tiled::build_maps_r<S, 1>(g, p, v, t); break;                                      \
+            case 2: ok = tiled::build_maps_r<S, 2>(g, p, v, t); break;                                      \
+            case 3: ok = tiled::build_maps_r<S, 3>(g, p, v, t); break;                                      \
+            case 4: ok = tiled::build_maps_r<S, 4>(g, p, v, t); break;                                      \
+        }                                                                                                  \
+        return ok ? cudaSuccess : cudaErrorInvalidValue;                                                   \
+    }                                                                                                      \
+    template <>                                                                                            \
+    cudaError_t launch_tiled<S>(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) { \
+        switch (g.R) {                                                                                     \
+            case 1: return tiled::launch_r<S, 1>(g, p, maps, vel, st);                                      \
+            case 2: return tiled::launch_r<S, 2>(g, p, maps, vel, st);                                      \
+            case 3: return tiled::launch_r<S, 3>(g, p, maps, vel, st);                                      \
+            case 4: return tiled::launch_r<S, 4>(g, p, maps, vel, st);                                      \
+        }                                                                                                  \
+        return cudaErrorInvalidValue;                                                                      \
+    }
+
+}  // namespace behf
