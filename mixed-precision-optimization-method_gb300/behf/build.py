@@ -49,10 +49,15 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
-    """Compile (incrementally) and return the path of libbehf.so."""
-    BUILD.mkdir(exist_ok=True)
-    LIBDIR.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None,
+          lib: Path | None = None, objdir: Path | None = None) -> Path:
+    """Compile (incrementally) and return the path of libbehf.so.
+
+    lib / objdir redirect the output (a build with different compile-time options next to the in-tree one)."""
+    LIB = Path(lib) if lib else globals()["LIB"]
+    BUILD = Path(objdir) if objdir else globals()["BUILD"]
+    BUILD.mkdir(parents=True, exist_ok=True)
+    LIB.parent.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     headers = _headers()
     objs = []

@@ -64,21 +64,13 @@ struct Geo {
 
 constexpr int al128(int b) { return (b + 127) & ~127; }
 
-// Stage layouts: see VOff / TOff in kernels_tiled_impl.cuh.  Velocity stage: halo boxes txx(X) tyy(Y)
-// txy(XY) txz(X) tyz(Y) p(XY), own vx vy vz qx qy qz, coefficients VW1x..z (FP32) then VW2x..z VW3x..z
-// VU1x..z VU2x..z.  Stress stage: halo vx vy vz (XY) qx (X) qy (Y), own sxx syy szz sxy sxz syz p,
-// coefficients P1 P2 S1 S2 S3 Sxy Sxz Syz.  Every region starts on a 128-byte boundary.
 struct VMaps {
     CUtensorMap halo[6];  // txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY)
-    CUtensorMap own[6];   // vx vy vz qx qy qz
-    CUtensorMap coef[15]; // VW1x..z VW2x..z VW3x..z VU1x..z VU2x..z
-    CUtensorMap zlead[4]; // tzz txz tyz p, own-cell box at plane k+R
+    CUtensorMap zlead[4]; // tzz txz tyz p: own-cell boxes for the z ring
 };
 struct TMaps {
     CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
-    CUtensorMap own[7];   // sxx syy szz sxy sxz syz p
-    CUtensorMap coef[8];  // P1 P2 S1 S2 S3 Sxy Sxz Syz
-    CUtensorMap zlead[4]; // vx vy vz qz, own-cell box at plane k+R
+    CUtensorMap zlead[4]; // vx vy vz qz: own-cell boxes for the z ring
 };
 
 // ------------------------------------------------------------------------------------- PTX helpers
@@ -92,22 +84,25 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// try_wait with a suspend-time hint: the hardware parks the waiting warp (up to `ns` nanoseconds) instead of
+// letting it spin, so waiting warps do not take issue slots from the warps that compute.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity, uint32_t ns) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false after kSpinLimit cycles.
+// Bounded wait: false once kSpinLimit cycles have passed (the clock is read every 256 polls).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity, 1000000u)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kSpinLimit) return false;
-    return true;
+    for (unsigned n = 1;; n++) {
+        if (mbar_try_wait(bar, parity, 1000000u)) return true;
+        if ((n & 255u) == 0 && clock64() - t0 > kSpinLimit) return false;
+    }
 }
 __device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
     asm volatile(
@@ -120,6 +115,9 @@ __device__ __forceinline__ void fence_init() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void fence_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
 // ------------------------------------------------------------------------------------- pair math
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }

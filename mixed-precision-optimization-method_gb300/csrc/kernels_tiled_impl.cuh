@@ -10,44 +10,48 @@
 namespace behf {
 namespace tiled {
 
-// Pipeline depth: stages in the shared-memory ring (NS - 1 planes in flight while one is computed).
+// Pipeline depth: NS stages in the shared-memory ring (NS - 1 planes in flight while one is computed), and
+// the CTAs per SM the launch bounds aim for (registers capped at 65536 / (256 MINB)).
+#ifndef BEHF_TILED_NS16
+#define BEHF_TILED_NS16 2
+#endif
+#ifndef BEHF_TILED_MINB16
+#define BEHF_TILED_MINB16 2
+#endif
+#ifndef BEHF_TILED_NS32
+#define BEHF_TILED_NS32 2
+#endif
+#ifndef BEHF_TILED_MINB32
+#define BEHF_TILED_MINB32 1
+#endif
 template <class S> struct Depth {
-    static constexpr int NS = sizeof(S) == 2 ? 3 : 2;
-    static constexpr int MINB = sizeof(S) == 2 ? 2 : 1;  // CTAs per SM the launch bounds aim for
+    static constexpr int NS = sizeof(S) == 2 ? BEHF_TILED_NS16 : BEHF_TILED_NS32;
+    static constexpr int MINB = sizeof(S) == 2 ? BEHF_TILED_MINB16 : BEHF_TILED_MINB32;
 };
+constexpr int NWARP = NTH / 32;
 
-// Byte offsets inside one stage.  Velocity: halo txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY), own
-// vx vy vz qx qy qz, VW1x..z (FP32), VW3x..z VU1x..z VU2x..z (VW2 = VU2 VW3 c_vw2 is derived), then the
-// z-queue fields at plane k+R (the queue's leading plane).
-template <class S, int R>
-struct VOff {
+// Shared-memory map of one CTA.  NS stages holding the halo boxes of plane k, then the z ring: for each of
+// the four fields with a z-derivative, ZS = 2R + NS own-cell boxes holding plane z at slot z % ZS (the window
+// k-R..k+R of the plane being computed plus the planes the producer has already requested).  A cell's own
+// fields and coefficients are read by its thread straight from global memory (coalesced pair loads issued
+// before the stencil work), so only data shared between threads goes through shared memory.
+//   velocity stage: txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY);  ring: tzz txz tyz p
+//   stress stage:   vx vy vz (XY) qx (X) qy (Y);                ring: vx vy vz qz
+template <class S, int R, bool VEL>
+struct Map {
     typedef Geo<S, R> G;
-    static constexpr int X = al128(G::X_B), Y = al128(G::Y_B), XY = al128(G::XY_B);
+    static constexpr int NS = Depth<S>::NS;
+    static constexpr int ZS = 2 * R + NS;
+    static constexpr int X = al128(G::X_B), Y = al128(G::Y_B), XY = al128(G::XY_B), OW = al128(G::OWN_B);
     __host__ __device__ static constexpr int halo(int i) {
-        return i == 0 ? 0 : i == 1 ? X : i == 2 ? X + Y : i == 3 ? X + Y + XY : i == 4 ? 2 * X + Y + XY : 2 * X + 2 * Y + XY;
+        return VEL ? (i == 0 ? 0 : i == 1 ? X : i == 2 ? X + Y : i == 3 ? X + Y + XY : i == 4 ? 2 * X + Y + XY
+                                                                                       : 2 * X + 2 * Y + XY)
+                   : (i < 3 ? i * XY : i == 3 ? 3 * XY : 3 * XY + X);
     }
-    static constexpr int own = 2 * X + 2 * Y + 2 * XY;
-    static constexpr int wof = own + 6 * al128(G::OWN_B);
-    static constexpr int kof = wof + 3 * al128(G::WOWN_B);
-    static constexpr int NK = 9;
-    static constexpr int zof = kof + NK * al128(G::KOWN_B);  // z-queue leading plane k+R: tzz txz tyz p
-    static constexpr int stage = zof + 4 * al128(G::OWN_B);
-    static constexpr uint32_t bytes =
-        2 * (G::X_B + G::Y_B + G::XY_B) + 10 * G::OWN_B + 3 * G::WOWN_B + NK * G::KOWN_B;
-};
-// Stress: halo vx vy vz (XY) qx (X) qy (Y), own sxx syy szz sxy sxz syz p, P1 P2 S1 S2 Sxy Sxz Syz.
-// (S3 = P1 c_s3 is derived.)
-template <class S, int R>
-struct TOff {
-    typedef Geo<S, R> G;
-    static constexpr int X = al128(G::X_B), Y = al128(G::Y_B), XY = al128(G::XY_B);
-    __host__ __device__ static constexpr int halo(int i) { return i < 3 ? i * XY : i == 3 ? 3 * XY : 3 * XY + X; }
-    static constexpr int own = 3 * XY + X + Y;
-    static constexpr int kof = own + 7 * al128(G::OWN_B);
-    static constexpr int NK = 7;
-    static constexpr int zof = kof + NK * al128(G::KOWN_B);  // z-queue leading plane k+R: vx vy vz qz
-    static constexpr int stage = zof + 4 * al128(G::OWN_B);
-    static constexpr uint32_t bytes = 3 * G::XY_B + G::X_B + G::Y_B + 11 * G::OWN_B + NK * G::KOWN_B;
+    static constexpr int stage = VEL ? 2 * X + 2 * Y + 2 * XY : 3 * XY + X + Y;
+    static constexpr int ring = NS * stage;            // z ring: [field][slot] boxes of OW bytes
+    static constexpr int bytes = ring + 4 * ZS * OW;
+    static constexpr uint32_t stage_tx = VEL ? 2 * (G::X_B + G::Y_B + G::XY_B) : 3 * G::XY_B + G::X_B + G::Y_B;
 };
 
 __device__ __forceinline__ float comp(float2 v, int c) { return c ? v.y : v.x; }
@@ -159,22 +163,52 @@ __device__ __forceinline__ void store_pair(S* dst, typename Pair<S>::T v, bool a
     }
 }
 
-// mbarrier ring of NS stages: phase bit s is the parity of stage s's next completion.
+// Single-producer pipeline: thread 0 issues every TMA; each warp releases a stage after reading it (one
+// arrival per warp on empty[s]); the producer refills a stage only after all eight warps released it.
+// Waits are bounded; phase bits track the parity of each barrier's next completion.
 template <int NS>
-struct Ring {
-    uint64_t* bar;
-    uint32_t phase;
-    __device__ __forceinline__ bool wait(int st) { return mbar_wait(&bar[st], (phase >> st) & 1u); }
-    __device__ __forceinline__ void advance(int st) { phase ^= 1u << st; }
-    // drain every stage with copies in flight (issued for planes k .. k+NS-2), each wait bounded
-    __device__ __forceinline__ void drain(int it, int k, int ke) {
-        for (int j = 0; j < NS - 1 && k + j < ke; j++) {
-            const int st = (it + j) % NS;
-            mbar_wait(&bar[st], (phase >> st) & 1u);
-            phase ^= 1u << st;
-        }
-    }
+struct Pipe {
+    uint64_t* full;
+    uint64_t* empty;
+    uint32_t fph = 0, eph = 0;
+    int pend[NS];  // producer: issued but not yet consumed by thread 0 (for the drain on error)
 };
+
+template <class M, class Issue>
+__device__ __forceinline__ bool producer_step(Pipe<M::NS>& pp, int it, int k, int kb, int ke, Issue&& issue) {
+    constexpr int NS = M::NS;
+    if (k + NS - 1 >= ke) return true;
+    const int sp = (it + NS - 1) % NS;
+    if (it >= 1) {  // the stage was used by step it-1: wait until every warp released it
+        if (!mbar_wait(&pp.empty[sp], (pp.eph >> sp) & 1u)) return false;
+        pp.eph ^= 1u << sp;
+    }
+    fence_async();
+    issue(sp, k + NS - 1, k + NS - 1 == kb);  // the first plane also brings the z-ring warm-up
+    pp.pend[sp]++;
+    return true;
+}
+
+template <class M>
+__device__ __forceinline__ void producer_drain(Pipe<M::NS>& pp) {
+#pragma unroll
+    for (int s = 0; s < M::NS; s++)
+        for (int n = 0; n < pp.pend[s]; n++) {
+            mbar_wait(&pp.full[s], (pp.fph >> s) & 1u);
+            pp.fph ^= 1u << s;
+        }
+}
+
+// Byte offsets of the z-ring slots of planes k-R .. k+R (shared by the four fields).
+template <class M, int R>
+__device__ __forceinline__ void ring_slots(int k, int* off) {
+    int s = (k - R) % M::ZS;
+#pragma unroll
+    for (int d = 0; d <= 2 * R; d++) {
+        off[d] = s * M::OW;
+        s = (s + 1 == M::ZS) ? 0 : s + 1;
+    }
+}
 
 // ----------------------------------------------------------------------------------------- velocity
 template <class S, int R>
@@ -185,10 +219,10 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     typedef typename Traits<S>::K K;
     typedef typename Pair<K>::T KP;
     typedef Geo<S, R> G;
-    typedef VOff<S, R> O;
-    constexpr int NS = Depth<S>::NS;
+    typedef Map<S, R, true> M;
+    constexpr int NS = M::NS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar[NS];
+    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS];
     // TMA destinations start on 128-byte boundaries: round the dynamic base up (128 B are reserved for it)
     unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
@@ -201,78 +235,84 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     const bool a0 = x >= R && x < g.nx - R, a1 = x + 1 >= R && x + 1 < g.nx - R;
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
+    const int oe = ty * TXC + xl;  // element offset of the pair in an own-cell box
 
     if (tid == 0) {
-        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        for (int s = 0; s < NS; s++) {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], NWARP);
+        }
         fence_init();
     }
     __syncthreads();
 
-    auto issue = [&](int st, int k) {
-        unsigned char* b = smem + st * O::stage;
-        uint64_t* br = &bar[st];
-        mbar_expect_tx(br, O::bytes);
-        tma3(b + O::halo(0), &maps.halo[0], br, x0 - G::HX, y0, k);      // txx  (x halo)
-        tma3(b + O::halo(1), &maps.halo[1], br, x0, y0 - R, k);          // tyy  (y halo)
-        tma3(b + O::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // txy  (x, y halo)
-        tma3(b + O::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // txz  (x halo)
-        tma3(b + O::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // tyz  (y halo)
-        tma3(b + O::halo(5), &maps.halo[5], br, x0 - G::HX, y0 - R, k);  // p    (x, y halo)
+    // z ring fields: tzz (forward), txz (backward), tyz (backward), p (forward)
+    auto issue = [&](int st, int k, bool warm) {
+        unsigned char* b = smem + st * M::stage;
+        uint64_t* br = &bfull[st];
+        mbar_expect_tx(br, M::stage_tx + 4 * G::OWN_B * (warm ? 2 * R + 1 : 1));
+        tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0, k);      // txx  (x halo)
+        tma3(b + M::halo(1), &maps.halo[1], br, x0, y0 - R, k);          // tyy  (y halo)
+        tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // txy  (x, y halo)
+        tma3(b + M::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // txz  (x halo)
+        tma3(b + M::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // tyz  (y halo)
+        tma3(b + M::halo(5), &maps.halo[5], br, x0 - G::HX, y0 - R, k);  // p    (x, y halo)
+        const int z0 = warm ? k - R : k + R;
+        for (int z = z0; z <= k + R; z++)
 #pragma unroll
-        for (int q = 0; q < 6; q++) tma3(b + O::own + q * al128(G::OWN_B), &maps.own[q], br, x0, y0, k);
-#pragma unroll
-        for (int q = 0; q < 3; q++) tma3(b + O::wof + q * al128(G::WOWN_B), &maps.coef[q], br, x0, y0, k);
-#pragma unroll
-        for (int q = 0; q < O::NK; q++)  // VW3x..z VU1x..z VU2x..z
-            tma3(b + O::kof + q * al128(G::KOWN_B), &maps.coef[6 + q], br, x0, y0, k);
-#pragma unroll
-        for (int q = 0; q < 4; q++) tma3(b + O::zof + q * al128(G::OWN_B), &maps.zlead[q], br, x0, y0, k + R);
+            for (int f = 0; f < 4; f++)
+                tma3(smem + M::ring + (f * M::ZS + z % M::ZS) * M::OW, &maps.zlead[f], br, x0, y0, z);
     };
 
-    // z queues: tzz (forward), txz (backward), tyz (backward), p (forward).  Q[f][d] = plane k-R+d for
-    // d < 2R in registers; plane k+R (d = 2R) comes with the stage.
-    const S* qsrc[4] = {reinterpret_cast<const S*>(p.f[BEHF_SZZ]), reinterpret_cast<const S*>(p.f[BEHF_SXZ]),
-                        reinterpret_cast<const S*>(p.f[BEHF_SYZ]), reinterpret_cast<const S*>(p.f[BEHF_P])};
-    P Q[4][2 * R];
-    if (live) {
-#pragma unroll
-        for (int f = 0; f < 4; f++)
-#pragma unroll
-            for (int d = 0; d < 2 * R; d++)
-                Q[f][d] = *reinterpret_cast<const P*>(qsrc[f] + (long long)(kb - R + d) * g.plane + col);
-    }
+    Pipe<NS> pp{bfull, bempty};
+    for (int s = 0; s < NS; s++) pp.pend[s] = 0;
     if (tid == 0)
-        for (int j = 0; j < NS - 1 && kb + j < ke; j++) issue(j, kb + j);
-    Ring<NS> ring{bar, 0u};
+        for (int j = 0; j < NS - 1 && kb + j < ke; j++) {
+            issue(j, kb + j, j == 0);
+            pp.pend[j]++;
+        }
+    bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it % NS;
-        const bool ok = ring.wait(st);
-        if (__syncthreads_or(!ok)) {
-            if (!ok) atomicExch(g.err, 1);
-            if (tid == 0) ring.drain(it, k, ke);
-            return;
+        bool ok = true;
+        if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
+        if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
+        if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform exit: every lane leaves together
+            failed = true;
+            break;
         }
-        ring.advance(st);
-        if (tid == 0 && k + NS - 1 < ke) {
-            fence_async();
-            issue((it + NS - 1) % NS, k + NS - 1);
-        }
-        const unsigned char* b = smem + st * O::stage;
-        const int oe = ty * TXC + xl;  // element offset of the pair in an own-cell box
+        pp.fph ^= 1u << st;
+        if (tid == 0) pp.pend[st]--;
+        const unsigned char* b = smem + st * M::stage;
         if (live) {
-            const S* txx = reinterpret_cast<const S*>(b + O::halo(0));
-            const S* tyy = reinterpret_cast<const S*>(b + O::halo(1));
-            const S* txy = reinterpret_cast<const S*>(b + O::halo(2));
-            const S* txz = reinterpret_cast<const S*>(b + O::halo(3));
-            const S* tyz = reinterpret_cast<const S*>(b + O::halo(4));
-            const S* pp = reinterpret_cast<const S*>(b + O::halo(5));
+            const long long go = (long long)k * g.plane + col;
+            // private data first: v, q, VW1 (FP32), VW3, VU1, VU2 -- consumed after the stencils
+            P vo_s[3], qo_s[3];
+            float2 vw1[3];
+            KP kw3[3], ku1[3], ku2[3], kw3y;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
+                qo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_QX + a]) + go);
+                vw1[a] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.k[VW1X + a]) + go);
+                kw3[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VW3X + a]) + go);
+                ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
+                ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
+            }
+            kw3y = kw3[1];
+            const S* txx = reinterpret_cast<const S*>(b + M::halo(0));
+            const S* tyy = reinterpret_cast<const S*>(b + M::halo(1));
+            const S* txy = reinterpret_cast<const S*>(b + M::halo(2));
+            const S* txz = reinterpret_cast<const S*>(b + M::halo(3));
+            const S* tyz = reinterpret_cast<const S*>(b + M::halo(4));
+            const S* pp_ = reinterpret_cast<const S*>(b + M::halo(5));
             const int rX = ty * G::BW + G::HX + xl;          // X box: row ty
             const int rXY = (ty + R) * G::BW + G::HX + xl;   // XY box: row ty + R
             const int rY = (ty + R) * TXC + xl;              // Y box: row ty + R
             XWin<S, R> w;
             w.load(txx + rX);
             float2 x1 = w.fwd();
-            w.load(pp + rXY);
+            w.load(pp_ + rXY);
             float2 s1 = w.fwd();
             w.load(txy + rXY);
             float2 y2 = w.bwd();
@@ -281,16 +321,18 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             float2 cv[2 * R + 1];
             load_col<S, R>(cv, tyy + rY, TXC);
             float2 y1 = col_fwd<R>(cv);
-            load_col<S, R>(cv, pp + rXY, G::BW);
+            load_col<S, R>(cv, pp_ + rXY, G::BW);
             float2 s2 = col_fwd<R>(cv);
             load_col<S, R>(cv, txy + rXY, G::BW);
             float2 x2 = col_bwd<R>(cv);
             load_col<S, R>(cv, tyz + rY, TXC);
             float2 z3 = col_bwd<R>(cv);
+            int zo[2 * R + 1];
+            ring_slots<M, R>(k, zo);
             auto zcol = [&](int f) {
+                const unsigned char* rb = smem + M::ring + f * M::ZS * M::OW + oe * sizeof(S);
 #pragma unroll
-                for (int d = 0; d < 2 * R; d++) cv[d] = PS::f2(Q[f][d]);
-                cv[2 * R] = PS::f2(*reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S)));
+                for (int d = 0; d <= 2 * R; d++) cv[d] = PS::f2(*reinterpret_cast<const P*>(rb + zo[d]));
             };
             zcol(0);
             float2 z1 = col_fwd<R>(cv);
@@ -309,41 +351,30 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
-            auto kc = [&](int q, int j) {  // stage slot q, multiplier of coefficient j
-                const KP kv = *reinterpret_cast<const KP*>(b + O::kof + q * al128(G::KOWN_B) + oe * sizeof(K));
-                return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j]));
-            };
-            const long long go = (long long)k * g.plane + col;
+            auto km = [&](KP kv, int j) { return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j])); };
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                const P qo_s = *reinterpret_cast<const P*>(b + O::own + (3 + a) * al128(G::OWN_B) + oe * sizeof(S));
-                const P vo_s = *reinterpret_cast<const P*>(b + O::own + a * al128(G::OWN_B) + oe * sizeof(S));
-                const float2 vw1 = *reinterpret_cast<const float2*>(b + O::wof + a * al128(G::WOWN_B) + oe * 4);
-                const float2 vw3 = kc(a, VW3X + a);
-                const float2 vu1 = kc(3 + a, VU1X + a), vu2 = kc(6 + a, VU2X + a);
+                const float2 vw3 = km(kw3[a], VW3X + a);
+                const float2 vu1 = km(ku1[a], VU1X + a), vu2 = km(ku2[a], VU2X + a);
                 const float2 vw2 = mul2(mul2(vu2, vw3), f2(g.c_vw2, g.c_vw2));
-                const float2 vw3p = (a == 2 && g.bug) ? kc(1, VW3Y) : vw3;  // reference: vz uses VW3y
-                const float2 qo = PS::f2(qo_s);
+                const float2 vw3p = (a == 2 && g.bug) ? km(kw3y, VW3Y) : vw3;  // reference: vz uses VW3y
+                const float2 qo = PS::f2(qo_s[a]);
                 // q' = VW1 q - VW2 sum(d sigma) - VW3 d p
                 const float2 t = fma2(vw2, sum[a], mul2(vw3p, dp[a]));
-                const float2 qn = fma2(vw1, qo, make_float2(-t.x, -t.y));
+                const float2 qn = fma2(vw1[a], qo, make_float2(-t.x, -t.y));
                 const P qs = PS::pack(qn);
                 store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_QX + a]) + go, qs, a0, a1);
                 // v' = v + VU1 sum(d sigma) - VU2 (q' - q)
                 const float2 dq = sub2(PS::f2(qs), qo);
-                const float2 vn = fma2(vu1, sum[a], fma2(make_float2(-vu2.x, -vu2.y), dq, PS::f2(vo_s)));
+                const float2 vn = fma2(vu1, sum[a], fma2(make_float2(-vu2.x, -vu2.y), dq, PS::f2(vo_s[a])));
                 store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, PS::pack(vn), a0, a1);
             }
         }
-        if (live && k + 1 < ke) {
-#pragma unroll
-            for (int f = 0; f < 4; f++) {
-#pragma unroll
-                for (int d = 0; d < 2 * R - 1; d++) Q[f][d] = Q[f][d + 1];
-                Q[f][2 * R - 1] = *reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S));
-            }
-        }
+        __syncwarp();
+        if (tx == 0) mbar_arrive(&bempty[st]);
     }
+    if (failed) atomicExch(g.err, 1);
+    if (tid == 0) producer_drain<M>(pp);
 }
 
 // ----------------------------------------------------------------------------------------- stress
@@ -355,10 +386,10 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     typedef typename Traits<S>::K K;
     typedef typename Pair<K>::T KP;
     typedef Geo<S, R> G;
-    typedef TOff<S, R> O;
-    constexpr int NS = Depth<S>::NS;
+    typedef Map<S, R, false> M;
+    constexpr int NS = M::NS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar[NS];
+    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS];
     unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -370,69 +401,70 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     const bool a0 = x >= R && x < g.nx - R, a1 = x + 1 >= R && x + 1 < g.nx - R;
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
+    const int oe = ty * TXC + xl;
 
     if (tid == 0) {
-        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        for (int s = 0; s < NS; s++) {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], NWARP);
+        }
         fence_init();
     }
     __syncthreads();
 
-    auto issue = [&](int st, int k) {
-        unsigned char* b = smem + st * O::stage;
-        uint64_t* br = &bar[st];
-        mbar_expect_tx(br, O::bytes);
-        tma3(b + O::halo(0), &maps.halo[0], br, x0 - G::HX, y0 - R, k);  // vx (x, y halo)
-        tma3(b + O::halo(1), &maps.halo[1], br, x0 - G::HX, y0 - R, k);  // vy
-        tma3(b + O::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
-        tma3(b + O::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // qx (x halo)
-        tma3(b + O::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // qy (y halo)
+    // z ring fields: vx (forward), vy (forward), vz (backward), qz (backward)
+    auto issue = [&](int st, int k, bool warm) {
+        unsigned char* b = smem + st * M::stage;
+        uint64_t* br = &bfull[st];
+        mbar_expect_tx(br, M::stage_tx + 4 * G::OWN_B * (warm ? 2 * R + 1 : 1));
+        tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0 - R, k);  // vx (x, y halo)
+        tma3(b + M::halo(1), &maps.halo[1], br, x0 - G::HX, y0 - R, k);  // vy
+        tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
+        tma3(b + M::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // qx (x halo)
+        tma3(b + M::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // qy (y halo)
+        const int z0 = warm ? k - R : k + R;
+        for (int z = z0; z <= k + R; z++)
 #pragma unroll
-        for (int q = 0; q < 7; q++) tma3(b + O::own + q * al128(G::OWN_B), &maps.own[q], br, x0, y0, k);
-#pragma unroll
-        for (int q = 0; q < O::NK; q++) {  // P1 P2 S1 S2 Sxy Sxz Syz (map order P1 P2 S1 S2 S3 Sxy Sxz Syz)
-            const int m = q < 4 ? q : q + 1;
-            tma3(b + O::kof + q * al128(G::KOWN_B), &maps.coef[m], br, x0, y0, k);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) tma3(b + O::zof + q * al128(G::OWN_B), &maps.zlead[q], br, x0, y0, k + R);
+            for (int f = 0; f < 4; f++)
+                tma3(smem + M::ring + (f * M::ZS + z % M::ZS) * M::OW, &maps.zlead[f], br, x0, y0, z);
     };
 
-    // z queues: vx (forward), vy (forward), vz (backward), qz (backward); registers hold planes k-R..k+R-1,
-    // the stage holds plane k+R.
-    const S* qsrc[4] = {reinterpret_cast<const S*>(p.f[BEHF_VX]), reinterpret_cast<const S*>(p.f[BEHF_VY]),
-                        reinterpret_cast<const S*>(p.f[BEHF_VZ]), reinterpret_cast<const S*>(p.f[BEHF_QZ])};
-    P Q[4][2 * R];
-    if (live) {
-#pragma unroll
-        for (int f = 0; f < 4; f++)
-#pragma unroll
-            for (int d = 0; d < 2 * R; d++)
-                Q[f][d] = *reinterpret_cast<const P*>(qsrc[f] + (long long)(kb - R + d) * g.plane + col);
-    }
+    Pipe<NS> pp{bfull, bempty};
+    for (int s = 0; s < NS; s++) pp.pend[s] = 0;
     if (tid == 0)
-        for (int j = 0; j < NS - 1 && kb + j < ke; j++) issue(j, kb + j);
-    Ring<NS> ring{bar, 0u};
+        for (int j = 0; j < NS - 1 && kb + j < ke; j++) {
+            issue(j, kb + j, j == 0);
+            pp.pend[j]++;
+        }
+    bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it % NS;
-        const bool ok = ring.wait(st);
-        if (__syncthreads_or(!ok)) {
-            if (!ok) atomicExch(g.err, 1);
-            if (tid == 0) ring.drain(it, k, ke);
-            return;
+        bool ok = true;
+        if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
+        if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
+        if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform exit: every lane leaves together
+            failed = true;
+            break;
         }
-        ring.advance(st);
-        if (tid == 0 && k + NS - 1 < ke) {
-            fence_async();
-            issue((it + NS - 1) % NS, k + NS - 1);
-        }
-        const unsigned char* b = smem + st * O::stage;
-        const int oe = ty * TXC + xl;
+        pp.fph ^= 1u << st;
+        if (tid == 0) pp.pend[st]--;
+        const unsigned char* b = smem + st * M::stage;
         if (live) {
-            const S* vx = reinterpret_cast<const S*>(b + O::halo(0));
-            const S* vy = reinterpret_cast<const S*>(b + O::halo(1));
-            const S* vz = reinterpret_cast<const S*>(b + O::halo(2));
-            const S* qx = reinterpret_cast<const S*>(b + O::halo(3));
-            const S* qy = reinterpret_cast<const S*>(b + O::halo(4));
+            const long long go = (long long)k * g.plane + col;
+            // private data first: the seven stresses/pressure and P1 P2 S1 S2 Sxy Sxz Syz
+            P so_s[7];
+            KP kk[7];
+#pragma unroll
+            for (int q = 0; q < 7; q++) {
+                so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
+                const int j = q < 4 ? P1 + q : P1 + q + 1;  // skip S3 (= P1 c_s3)
+                kk[q] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[j]) + go);
+            }
+            const S* vx = reinterpret_cast<const S*>(b + M::halo(0));
+            const S* vy = reinterpret_cast<const S*>(b + M::halo(1));
+            const S* vz = reinterpret_cast<const S*>(b + M::halo(2));
+            const S* qx = reinterpret_cast<const S*>(b + M::halo(3));
+            const S* qy = reinterpret_cast<const S*>(b + M::halo(4));
             const int rX = ty * G::BW + G::HX + xl;
             const int rXY = (ty + R) * G::BW + G::HX + xl;
             const int rY = (ty + R) * TXC + xl;
@@ -454,10 +486,12 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             float2 uzy = col_fwd<R>(cv);
             load_col<S, R>(cv, qy + rY, TXC);
             float2 wy = col_bwd<R>(cv);
+            int zo[2 * R + 1];
+            ring_slots<M, R>(k, zo);
             auto zcol = [&](int f) {
+                const unsigned char* rb = smem + M::ring + f * M::ZS * M::OW + oe * sizeof(S);
 #pragma unroll
-                for (int d = 0; d < 2 * R; d++) cv[d] = PS::f2(Q[f][d]);
-                cv[2 * R] = PS::f2(*reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S)));
+                for (int d = 0; d <= 2 * R; d++) cv[d] = PS::f2(*reinterpret_cast<const P*>(rb + zo[d]));
             };
             zcol(2);
             float2 uzz = col_bwd<R>(cv);
@@ -475,18 +509,15 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);
-            auto kc = [&](int q, int j) {
-                const KP kv = *reinterpret_cast<const KP*>(b + O::kof + q * al128(G::KOWN_B) + oe * sizeof(K));
-                return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j]));
+            auto kc = [&](int q) {
+                const int j = q < 4 ? P1 + q : P1 + q + 1;
+                return mul2(Pair<K>::f2(kk[q]), f2(g.kmulf[j], g.kmulf[j]));
             };
-            auto own = [&](int q) {
-                return PS::f2(*reinterpret_cast<const P*>(b + O::own + q * al128(G::OWN_B) + oe * sizeof(S)));
-            };
-            const long long go = (long long)k * g.plane + col;
+            auto own = [&](int q) { return PS::f2(so_s[q]); };
             auto put = [&](int field, float2 v) {
                 store_pair<S>(reinterpret_cast<S*>(p.f[field]) + go, PS::pack(v), a0, a1);
             };
-            const float2 p1 = kc(0, P1), p2 = kc(1, P2), g1 = kc(2, S1), g2 = kc(3, S2);
+            const float2 p1 = kc(0), p2 = kc(1), g1 = kc(2), g2 = kc(3);
             const float2 g3dq = mul2(mul2(p1, f2(g.c_s3, g.c_s3)), dq);  // S3 = P1 c_s3
             // p' = p - P1 div v - P2 div q
             put(BEHF_P, sub2(own(6), fma2(p1, dv, mul2(p2, dq))));
@@ -495,19 +526,15 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             put(BEHF_SYY, add2(own(1), fma2(g1, add2(uxx, uzz), fma2(g2, uyy, g3dq))));
             put(BEHF_SZZ, add2(own(2), fma2(g1, add2(uxx, uyy), fma2(g2, uzz, g3dq))));
             // s_ij' = s_ij + S_ij (d_j v_i + d_i v_j)
-            put(BEHF_SXY, fma2(kc(4, SXYC), add2(uxy, uyx), own(3)));
-            put(BEHF_SXZ, fma2(kc(5, SXZC), add2(uxz, uzx), own(4)));
-            put(BEHF_SYZ, fma2(kc(6, SYZC), add2(uyz, uzy), own(5)));
+            put(BEHF_SXY, fma2(kc(4), add2(uxy, uyx), own(3)));
+            put(BEHF_SXZ, fma2(kc(5), add2(uxz, uzx), own(4)));
+            put(BEHF_SYZ, fma2(kc(6), add2(uyz, uzy), own(5)));
         }
-        if (live && k + 1 < ke) {
-#pragma unroll
-            for (int f = 0; f < 4; f++) {
-#pragma unroll
-                for (int d = 0; d < 2 * R - 1; d++) Q[f][d] = Q[f][d + 1];
-                Q[f][2 * R - 1] = *reinterpret_cast<const P*>(b + O::zof + f * al128(G::OWN_B) + oe * sizeof(S));
-            }
-        }
+        __syncwarp();
+        if (tx == 0) mbar_arrive(&bempty[st]);
     }
+    if (failed) atomicExch(g.err, 1);
+    if (tid == 0) producer_drain<M>(pp);
 }
 
 // ----------------------------------------------------------------------------------------- host side
@@ -547,7 +574,6 @@ inline bool encode(CUtensorMap* m, const Geom& g, void* base, int bw, int bh) {
 template <class S, int R>
 bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     typedef Geo<S, R> G;
-    typedef typename Traits<S>::K K;
     bool ok = true;
     // velocity
     ok &= encode<S>(&vm->halo[0], g, p.f[BEHF_SXX], G::BW, TY);
@@ -556,9 +582,6 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     ok &= encode<S>(&vm->halo[3], g, p.f[BEHF_SXZ], G::BW, TY);
     ok &= encode<S>(&vm->halo[4], g, p.f[BEHF_SYZ], TXC, G::BH);
     ok &= encode<S>(&vm->halo[5], g, p.f[BEHF_P], G::BW, G::BH);
-    for (int q = 0; q < 6; q++) ok &= encode<S>(&vm->own[q], g, p.f[BEHF_VX + q], TXC, TY);
-    for (int q = 0; q < 3; q++) ok &= encode<float>(&vm->coef[q], g, p.k[q], TXC, TY);
-    for (int q = 3; q < 15; q++) ok &= encode<K>(&vm->coef[q], g, p.k[q], TXC, TY);
     ok &= encode<S>(&vm->zlead[0], g, p.f[BEHF_SZZ], TXC, TY);
     ok &= encode<S>(&vm->zlead[1], g, p.f[BEHF_SXZ], TXC, TY);
     ok &= encode<S>(&vm->zlead[2], g, p.f[BEHF_SYZ], TXC, TY);
@@ -569,8 +592,6 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     ok &= encode<S>(&tm->halo[2], g, p.f[BEHF_VZ], G::BW, G::BH);
     ok &= encode<S>(&tm->halo[3], g, p.f[BEHF_QX], G::BW, TY);
     ok &= encode<S>(&tm->halo[4], g, p.f[BEHF_QY], TXC, G::BH);
-    for (int q = 0; q < 7; q++) ok &= encode<S>(&tm->own[q], g, p.f[BEHF_SXX + q], TXC, TY);
-    for (int q = 0; q < 8; q++) ok &= encode<K>(&tm->coef[q], g, p.k[P1 + q], TXC, TY);
     ok &= encode<S>(&tm->zlead[0], g, p.f[BEHF_VX], TXC, TY);
     ok &= encode<S>(&tm->zlead[1], g, p.f[BEHF_VY], TXC, TY);
     ok &= encode<S>(&tm->zlead[2], g, p.f[BEHF_VZ], TXC, TY);
@@ -591,7 +612,6 @@ inline int num_sms() {
 
 template <class S, int R>
 cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) {
-    constexpr int NS = Depth<S>::NS;
     const int nbx = (g.nx - R + TXC - 1) / TXC, nby = (g.ny - R + TY - 1) / TY;
     const int planes = g.nz - 2 * R;
     // enough CTAs for every SM: split z into chunks when the xy tiling alone is too small
@@ -603,7 +623,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     const int zchunk = (planes + nzc - 1) / nzc;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
-        const int smem = NS * VOff<S, R>::stage + 128;
+        const int smem = Map<S, R, true>::bytes + 128;
         static bool attr = false;
         if (!attr) {
             cudaError_t e = cudaFuncSetAttribute(k_vel<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -612,7 +632,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
         }
         k_vel<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const VMaps*>(maps), g, p, zchunk);
     } else {
-        const int smem = NS * TOff<S, R>::stage + 128;
+        const int smem = Map<S, R, false>::bytes + 128;
         static bool attr = false;
         if (!attr) {
             cudaError_t e = cudaFuncSetAttribute(k_str<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
