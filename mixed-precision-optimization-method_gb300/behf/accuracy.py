@@ -1,0 +1,72 @@
+"""Full-size accuracy of the storage precisions: seismogram relative L2 per recorded field.
+
+    python -m behf.accuracy --workload layered256 [--steps 2000]
+        FP64 (the plain kernels, the GPU oracle run of the same scheme) vs FP32, FP16, BF16 (tiled kernels)
+    python -m behf.accuracy --workload random1024 [--steps 1200]
+        FP16 and BF16 vs FP32 (FP64 at 1024^3 does not fit one GPU; FP32 is within 1e-4 of FP64 on the
+        parity tests, so the FP16-vs-FP32 error stands for FP16-vs-FP64)
+
+Prints one JSON object: per precision and per recorded field the relative L2 error of all traces, the
+storage scales, the wall time, and the health check (NaN/Inf/saturation) at the end.  Runs the precisions
+one after another (one context on the device at a time).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import FIELDS, solver_for
+from . import problems
+
+
+def run_one(prob, precision: str, kernel: str = "auto"):
+    s = solver_for(prob, precision, kernel)
+    t0 = time.perf_counter()
+    s.run(prob.nt)
+    wall = time.perf_counter() - t0
+    seis = s.seismograms()
+    ok, _ = s.health()
+    info = s.info()
+    s.close()
+    return seis, {"wall_s": wall, "health_ok": bool(ok), "kernel": info["kernel"], "scales": info["scales"],
+                  "gpts": prob.cells * prob.nt / wall / 1e9}
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    den = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / den) if den > 0 else float("nan")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="layered256", choices=["layered256", "random1024", "small64"])
+    ap.add_argument("--steps", type=int, default=0)
+    ap.add_argument("--n", type=int, default=0, help="grid override (test-sized runs)")
+    args = ap.parse_args(argv)
+    if args.workload == "layered256":
+        prob = problems.layered256(n=args.n or 256, nt=args.steps or 2000)
+        ref_prec, others = "f64", ["f32", "f16", "bf16"]
+    elif args.workload == "small64":
+        prob = problems.small64(n=args.n or 64, nt=args.steps or 500)
+        ref_prec, others = "f64", ["f32", "f16", "bf16"]
+    else:
+        prob = problems.random1024(n=args.n or 1024, nt=args.steps or 1200, medium=False, nrec_side=128)
+        ref_prec, others = "f32", ["f16", "bf16"]
+    out = {"workload": prob.name, "cells": prob.cells, "steps": prob.nt, "reference": ref_prec, "runs": {}}
+    ref, meta = run_one(prob, ref_prec)
+    out["runs"][ref_prec] = meta
+    comps = np.unique(prob.rec_comp)
+    out["peak"] = {FIELDS[c]: float(np.abs(ref[prob.rec_comp == c]).max()) for c in comps}
+    for prec in others:
+        seis, meta = run_one(prob, prec)
+        meta["rel_l2"] = {FIELDS[c]: rel_l2(seis[prob.rec_comp == c], ref[prob.rec_comp == c]) for c in comps}
+        out["runs"][prec] = meta
+    print(json.dumps(out))
+    return out
+
+
+if __name__ == "__main__":
+    main()

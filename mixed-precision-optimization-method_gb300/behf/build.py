@@ -88,6 +88,35 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     return LIB
 
 
+DRIVER_SRC = ROOT / "driver" / "behf_main.cpp"
+DRIVER = LIBDIR / "behf_run"
+
+
+def cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("no C++ compiler found")
+
+
+def build_driver(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the command-line driver (host C++ only) against libbehf.so; the binary finds the library
+    next to itself (rpath $ORIGIN)."""
+    lib = build(verbose=verbose)
+    if force or _stale(DRIVER, [DRIVER_SRC, INCLUDE / "behf.h", lib, Path(__file__)]):
+        tmp = DRIVER.with_name(DRIVER.name + ".tmp")
+        cmd = [cxx(), "-std=c++17", "-O2", "-Wall", "-I", str(INCLUDE), str(DRIVER_SRC), "-o", str(tmp),
+               "-L", str(LIBDIR), "-lbehf", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose=True, extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None))
+    print(build_driver(force="--force" in sys.argv, verbose=True))

@@ -193,6 +193,22 @@ def ricker(nt: int, dt: float, f0: float, t0: float | None = None, amp: float = 
     return (amp * -(1 - 2 * a) * np.exp(-a)).astype(np.float32)
 
 
+def ricker_reference(nt: int, dt: float, f0: float) -> np.ndarray:
+    """The same wavelet evaluated as kernel.cu:1890-1898 does: t = it*DT and T0 = 1.2/F0 in float, the
+    product in double with pi = 3.1415926535, the result rounded to float."""
+    f32 = np.float32
+    DT, F0 = f32(dt), f32(f0)
+    T0 = f32(1.2 / float(F0))
+    pi = 3.1415926535
+    w = np.empty(nt, np.float32)
+    for it in range(nt):
+        d = float(f32(f32(it) * DT) - T0)
+        a2 = 2 * pi * pi * float(F0) * float(F0) * d * d
+        a = pi * pi * float(F0) * float(F0) * d * d
+        w[it] = f32(-(1 - a2) * np.exp(-a))
+    return w
+
+
 def homogeneous(shape, rock=SANDSTONE) -> np.ndarray:
     m = rock_moduli(**rock)
     return np.broadcast_to(m[:, None, None, None], (9, *shape)).astype(np.float32)
@@ -292,15 +308,16 @@ def borehole_moduli(nz, ny, nx) -> np.ndarray:
 
 
 def borehole(scale: float = 1.0, nt=3500) -> Problem:
-    """The reference's problem (main.cpp:20-23, 84-99), optionally shrunk by ``scale`` (cells)."""
-    NX, NY, NZ, NP = (max(24, int(round(v * scale))) for v in (180, 180, 300, 30))
+    """The reference's problem (main.cpp:20-23, 84-99), optionally shrunk by ``scale`` (cells): txx recorded
+    on the whole vertical line through the source (the reference's sisx files hold every z of that line)."""
+    NX, NY, NZ = (max(24, int(round(v * scale))) for v in (180, 180, 300))
     NP = max(4, int(round(30 * scale)))
     nx, ny, nz = NX + 2 * NP, NY + 2 * NP, NZ + 2 * NP
     h, dt, f0 = 0.01, 1e-6, 1e4
     sx, sy, sz = nx // 2, ny // 2, min(20 + NP, nz - NP - 2)
-    ijk, comp = line_receivers(sx, sy, np.arange(1, nz - 1), [6])
-    return Problem(nx, ny, nz, h, dt, 1, borehole_moduli(nz, ny, nx), ricker(nt, dt, f0), (sx, sy, sz), ijk, comp,
-                   cpml_width=NP, cpml_v0=4000.0, cpml_r=1e-6, f0=f0, ref_bug_compat=True,
+    ijk, comp = line_receivers(sx, sy, np.arange(0, nz), [6])
+    return Problem(nx, ny, nz, h, dt, 1, borehole_moduli(nz, ny, nx), ricker_reference(nt, dt, f0), (sx, sy, sz),
+                   ijk, comp, cpml_width=NP, cpml_v0=4000.0, cpml_r=1e-6, f0=f0, ref_bug_compat=True,
                    scales=(1e8, 1e8, 1.0, 1.0), name="borehole")
 
 

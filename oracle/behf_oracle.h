@@ -87,6 +87,18 @@ void orc_ricker(int nt, double dt, double f0, double t0, double amp, float* w);
 int orc_run(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
             int nrec, const int* rec_ijk, const int* rec_comp, double* seis, double* fields_out);
 
+/* FP64 discrete adjoint of orc_run (behf_adjoint.cpp), physical units (storage scales ignored).
+ * Runs the forward from rest with checkpoints every `stride` steps (<= 0: round(sqrt(nt))), then the
+ * adjoint with the adjoint source adj_src[nrec*nt] (dJ/d seismogram sample; NULL = zero) added at the
+ * receivers.  Outputs (each may be NULL): seis_out[nrec*nt] forward seismograms; grad_wavelet[nt]
+ * dJ/d wavelet sample; grad_coef[23*N] dJ/d effective coefficient (physical coefficient times 1/h where
+ * it multiplies a difference), accumulated over cells outside every CPML slab; grad_mod[9*N] dJ/d
+ * cell-centred moduli, exact on cells whose coefficient cells all lie outside the slabs, else 0.
+ * Returns 0, or negative on invalid input. */
+int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
+                int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
+                double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod);
+
 /* Wall seconds of the time-step loop of the last orc_run (set-up excluded); OpenMP thread count. */
 double orc_last_step_seconds(void);
 int orc_threads(void);

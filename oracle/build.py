@@ -1,6 +1,7 @@
 """Build recipe for the oracle (test infrastructure, the checker of the CUDA path).
 
-* ``build_oracle()`` compiles ``behf_oracle.cpp`` into ``oracle/_build/liboracle.so``.
+* ``build_oracle()`` compiles ``behf_oracle.cpp`` (forward) and ``behf_adjoint.cpp`` (FP64 discrete
+  adjoint) into ``oracle/_build/liboracle.so``.
 * ``build_ref()`` compiles the reference's own kernel bodies for the CPU into
   ``oracle/_ref/libbehf_ref.so``, linked with the reference's ``outputfunc.cpp`` (compiled
   where it lies) for its medium builder ``create_model_all``.  It reads ``kernel.cu`` from the reference tree, copies the
@@ -37,9 +38,10 @@ def _needs(out: Path, deps: list[Path]) -> bool:
 def build_oracle(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     out = BUILD / "liboracle.so"
-    deps = [HERE / "behf_oracle.cpp", HERE / "behf_oracle.h"]
+    srcs = [HERE / "behf_oracle.cpp", HERE / "behf_adjoint.cpp"]
+    deps = [*srcs, HERE / "behf_oracle.h"]
     if force or _needs(out, deps):
-        cmd = ["g++", *CXXFLAGS, "-o", str(out), str(HERE / "behf_oracle.cpp")]
+        cmd = ["g++", *CXXFLAGS, "-o", str(out), *map(str, srcs)]
         subprocess.run(cmd, check=True)
     return out
 

@@ -151,6 +151,49 @@ def run(prob, precision: str = "f64", nthreads: int = 0, nt: int | None = None,
     return seis, fo
 
 
+def _cfg(prob, precision="f64", nthreads=0):
+    cfg = OrcCfg()
+    cfg.nx, cfg.ny, cfg.nz, cfg.radius = prob.nx, prob.ny, prob.nz, prob.radius
+    cfg.h, cfg.dt = prob.h, prob.dt
+    cfg.precision = PRECISIONS[precision]
+    cfg.ref_bug_compat = int(prob.ref_bug_compat)
+    cfg.cpml_width, cfg.cpml_v0, cfg.cpml_r = prob.cpml_width, prob.cpml_v0, prob.cpml_r
+    for i in range(4):
+        cfg.scale[i] = 1.0
+    cfg.src_kind = SOURCES[prob.src_kind]
+    cfg.src_ix, cfg.src_iy, cfg.src_iz = prob.src
+    cfg.nthreads = nthreads
+    return cfg
+
+
+def adjoint(prob, adj_src=None, stride: int = 0, nt: int | None = None, want_coef: bool = False,
+            mod=None, nthreads: int = 0):
+    """FP64 discrete adjoint (behf_adjoint.cpp) of a problem description, physical units.
+
+    adj_src [nrec, nt]: dJ/d seismogram sample (None: zero).  mod overrides prob.mod.
+    Returns dict(seis [nrec, nt], grad_wavelet [nt], grad_mod [9, nz, ny, nx], grad_coef [23, ...] or None)."""
+    nt = prob.nt if nt is None else nt
+    cfg = _cfg(prob, "f64", nthreads)
+    mod = _c(prob.mod if mod is None else mod, np.float32)
+    w = _c(prob.wavelet[:nt], np.float32)
+    ri = _c(prob.rec_ijk, np.int32).reshape(-1)
+    rc = _c(prob.rec_comp, np.int32)
+    nrec = rc.shape[0]
+    adj = None if adj_src is None else _c(adj_src, np.float64).reshape(nrec, nt)
+    seis = np.zeros((nrec, nt), np.float64)
+    gw = np.zeros(nt, np.float64)
+    gmod = np.zeros((NMOD, prob.nz, prob.ny, prob.nx), np.float64)
+    gcoef = np.zeros((NCOEF, prob.nz, prob.ny, prob.nx), np.float64) if want_coef else None
+    D = lambda a: a.ctypes.data_as(_P(C.c_double)) if a is not None else None  # noqa: E731
+    lib().orc_adjoint.restype = C.c_int
+    rcode = lib().orc_adjoint(C.byref(cfg), _ptrs(list(mod), C.c_float), w.ctypes.data_as(_P(C.c_float)), nt, nrec,
+                              ri.ctypes.data_as(_P(C.c_int)), rc.ctypes.data_as(_P(C.c_int)), D(adj), int(stride),
+                              D(seis), D(gw), D(gcoef), D(gmod))
+    if rcode != 0:
+        raise ValueError(f"orc_adjoint failed with {rcode}")
+    return {"seis": seis, "grad_wavelet": gw, "grad_mod": gmod, "grad_coef": gcoef}
+
+
 def last_step_seconds() -> float:
     """Wall seconds of the time-step loop of the last run() (set-up excluded)."""
     return float(lib().orc_last_step_seconds())
