@@ -88,6 +88,9 @@ enum {
     BEHF_OPT_KERNEL = 0,         /* behf_kernel */
     BEHF_OPT_REF_BUG_COMPAT = 1, /* 1: vz Darcy update uses the y-staggered VW3 as kernel.cu:220 does */
     BEHF_OPT_GRAPH_CHUNK = 2,    /* steps per captured CUDA graph (0 = no graph) */
+    BEHF_OPT_GRADIENT = 3,       /* 1: keep the cell-centred moduli on the device (9 x 4 B per cell) so that
+                                    behf_gradient can map coefficient gradients to moduli; set before the medium */
+    BEHF_OPT_CHECKPOINT = 4,     /* steps between checkpoints of the gradient's forward pass (0 = round(sqrt(nt))) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current
@@ -192,6 +195,24 @@ behf_status behf_health(behf_ctx* ctx, double* norms);
  * calls share the array, so calls that overlap on the GPU race. */
 behf_status behf_field_norm_noalloc(const void* field, int precision, int nx, int ny, int nz, long long pitch,
                                     long long plane, double* norm_out, int* flag_out, void* stream);
+
+/* Adjoint-state gradient (no counterpart in the reference, which has no adjoint).  Runs the forward from rest
+ * over nt steps with checkpoints every BEHF_OPT_CHECKPOINT steps (full state: fields + CPML memory), then the
+ * exact discrete adjoint of the same steps backwards, recomputing one segment at a time from its checkpoint.
+ *   adj_src        [nrec][nt] host: dJ/d seismogram sample, physical units (the adjoint source)
+ *   grad_wavelet   [nt] host or NULL: dJ/d wavelet sample
+ *   grad_moduli    BEHF_NMOD host arrays [nz][ny][nx] (entries may be NULL): dJ/d cell-centred modulus, exact
+ *                  on cells whose staggered coefficient cells lie outside the CPML slabs and the ghost ring
+ *                  (the absorbing layers are not inverted), zero elsewhere.
+ * Needs BEHF_OPT_GRADIENT before the medium, a source, and receivers of capacity >= nt.  The adjoint runs in
+ * the context's arithmetic type (FP32 for the 16-bit kinds, FP64 for FP64).  Afterwards the seismograms are
+ * those of the forward pass (behf_get_seismograms); the wavefields are not meaningful (behf_reset). */
+behf_status behf_gradient(behf_ctx* ctx, int nt, const double* adj_src, double* grad_wavelet,
+                          double* const grad_moduli[BEHF_NMOD]);
+/* Same for the L2 misfit J = 1/2 sum (seis - observed)^2 (observed [nrec][nt] host, physical units): the
+ * adjoint source is the residual of the forward pass; J is written to *misfit. */
+behf_status behf_misfit_gradient(behf_ctx* ctx, int nt, const double* observed, double* misfit,
+                                 double* grad_wavelet, double* const grad_moduli[BEHF_NMOD]);
 
 /* Text of the last error on this thread. */
 const char* behf_last_error(void);

@@ -22,7 +22,7 @@ MODULI = ["rho", "rhof", "mu", "M", "C", "HH", "H2u", "C1", "C2"]
 PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
-OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK = 0, 1, 2
+OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT = 0, 1, 2, 3, 4
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -113,6 +113,9 @@ def load() -> C.CDLL:
         "behf_update_wavelet": [C.c_void_p, C.c_int, P(C.c_float), C.c_int],
         "behf_get_seismograms_range": [C.c_void_p, C.c_int, C.c_int, P(C.c_double)],
         "behf_time_kernels": [C.c_void_p, C.c_int, P(C.c_double)],
+        "behf_gradient": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double), P(P(C.c_double))],
+        "behf_misfit_gradient": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double),
+                                 P(P(C.c_double))],
         "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                     C.c_void_p, C.c_void_p, C.c_void_p],
     }
@@ -272,6 +275,38 @@ class Solver:
         _check(self._lib.behf_time_kernels(self._ctx, int(nsteps), ms.ctypes.data_as(C.POINTER(C.c_double))))
         return {"source": ms[0], "velocity": ms[1], "stress": ms[2], "record": ms[3]}
 
+    # -- gradient (adjoint state, checkpointed)
+    def enable_gradient(self, checkpoint: int = 0):
+        """Keep the moduli on the device for behf_gradient (call before the medium); checkpoint = steps
+        between checkpoints of the gradient's forward pass (0 = round(sqrt(nt)))."""
+        self.set_option(OPT_GRADIENT, 1)
+        self.set_option(OPT_CHECKPOINT, int(checkpoint))
+
+    def _grad_out(self, nt, moduli):
+        gw = np.zeros(nt, np.float64)
+        gm = np.zeros((9,) + self.shape, np.float64) if moduli else None
+        arr = (C.POINTER(C.c_double) * 9)(*[gm[q].ctypes.data_as(C.POINTER(C.c_double)) if moduli else None
+                                            for q in range(9)])
+        return gw, gm, arr
+
+    def gradient(self, nt: int, adj_src: np.ndarray, moduli: bool = True):
+        """Adjoint-state gradient for the adjoint source adj_src [nrec, nt] (dJ/d seismogram, physical units).
+        Returns (dJ/d wavelet [nt], dJ/d moduli [9, nz, ny, nx] or None)."""
+        adj = np.ascontiguousarray(adj_src, np.float64).reshape(self.nrec, nt)
+        gw, gm, arr = self._grad_out(nt, moduli)
+        _check(self._lib.behf_gradient(self._ctx, int(nt), adj.ctypes.data_as(C.POINTER(C.c_double)),
+                                       gw.ctypes.data_as(C.POINTER(C.c_double)), arr))
+        return gw, gm
+
+    def misfit_gradient(self, nt: int, observed: np.ndarray, moduli: bool = True):
+        """L2 misfit J = 1/2 |seis - observed|^2 and its gradient.  Returns (J, dJ/d wavelet, dJ/d moduli)."""
+        obs = np.ascontiguousarray(observed, np.float64).reshape(self.nrec, nt)
+        gw, gm, arr = self._grad_out(nt, moduli)
+        J = C.c_double(0)
+        _check(self._lib.behf_misfit_gradient(self._ctx, int(nt), obs.ctypes.data_as(C.POINTER(C.c_double)),
+                                              C.byref(J), gw.ctypes.data_as(C.POINTER(C.c_double)), arr))
+        return J.value, gw, gm
+
     def health(self):
         norms = np.zeros(13, np.float64)
         code = self._lib.behf_health(self._ctx, norms.ctypes.data_as(C.POINTER(C.c_double)))
@@ -313,8 +348,10 @@ def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:
     return {"velocity": vel, "stress": strs, "step_unfused": vel + strs, "step_fused": fused}
 
 
-def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None) -> Solver:
-    """A Solver set up with a problem description (see behf.problems.Problem)."""
+def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None, gradient=False,
+               checkpoint=0) -> Solver:
+    """A Solver set up with a problem description (see behf.problems.Problem); gradient=True keeps what
+    Solver.gradient needs."""
     s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
                cpml_width=prob.cpml_width, cpml_v0=prob.cpml_v0, cpml_r=prob.cpml_r, scales=scales,
                src_amp_hint=float(np.abs(prob.wavelet).max()) if prob.wavelet.size else 1.0,
@@ -322,6 +359,8 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None)
     if prob.ref_bug_compat:
         s.set_option(OPT_REF_BUG_COMPAT, 1)
     s.set_kernel(kernel)
+    if gradient:
+        s.enable_gradient(checkpoint)
     if prob.mod.shape[1:] == (prob.nz, prob.ny, prob.nx):
         s.set_medium(prob.mod)
     else:

@@ -1,0 +1,60 @@
+// behf_adjoint.cuh -- discrete adjoint of the BEHF step (adjoint.cu): device pointers and launchers.
+//
+// The forward step n is  source -> V -> force source -> T -> record,  linear in the state (13 fields in
+// storage units + CPML memory).  Its adjoint runs  record^T -> T^T -> force^T -> V^T -> source^T  on
+// adjoint fields of the forward arithmetic type A (float, or double for FP64 storage), and accumulates
+// the gradient with respect to each effective coefficient (stored value x power-of-two multiplier) on
+// cells outside every CPML slab.  Each of T^T and V^T is three launches:
+//   1. per cell: adjoints of the derivative groups (7 for T, 6 for V) into tmp[], coefficient gradients
+//      from the forward snapshot of this step;
+//   2. gather: each field's adjoint takes minus the transposed stencils of the derivative adjoints of its
+//      neighbours, each corrected on the fly by the adjoint CPML memory of the neighbour's slab;
+//   3. per slab cell: the adjoint CPML memory update  L = lpsi + lD;  lpsi = A L;  lprev = A B L.
+#pragma once
+#include "behf_internal.cuh"
+
+namespace behf {
+
+struct AdjPtrs {
+    void* lf[kNField];       // adjoint fields, type A, pitched like the forward fields
+    void* lpsi[3][8];        // adjoint CPML memory, type A, slab layout of the forward memory
+    void* lprv[3][8];
+    void* tmp[7];            // per-cell derivative-group adjoints, type A, pitched (zero off the updated cells)
+    void* g[kNCoef];         // gradient accumulators per effective coefficient, type A, pitched
+    const void* cur[kNField];  // forward snapshot of this step after V (and the force source), type S
+    const void* qprev[3];    // q before V of this step, type S
+    int grad;                // accumulate coefficient gradients
+};
+
+struct AdjScales {
+    double s[kNField];       // multiplier of the adjoint source per recorded field (alpha / storage scale)
+};
+
+// T^T and V^T of one step (three launches each).
+template <class S> cudaError_t adj_step_t(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st);
+template <class S> cudaError_t adj_step_v(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st);
+// record^T: lf[comp[r]][off[r]] += adj[r * nt + it] * sc.s[comp[r]]  (atomic: receivers may share a cell)
+template <class S>
+cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, int nrec, const double* adj, int nt,
+                       int it, const AdjScales& sc, cudaStream_t st);
+// source^T at one cell.  phase 0 (after T^T, force source): gw[it] = fac * lvz, gfac += w[it] * lvz (it < nw).
+// phase 1 (after V^T): explosive gw[it] = fac * (lsxx + lsyy + lszz), pressure gw[it] = fac * lp.
+template <class S>
+cudaError_t adj_point(const AdjPtrs& a, long long o, int kind, int phase, double fac, const float* w, int nw, int it,
+                      double* gw, double* gfac, cudaStream_t st);
+
+// Coefficient-build transpose (main.cpp:322-494 formulas): moduli gradient gm[9][nz][ny][nx] (double,
+// unpitched) from the effective-coefficient gradients g[] (ratio[] = effective / physical coefficient),
+// zero outside the cells whose coefficient cells c - {0,1}^3 all carry gradients.
+struct GradModArgs {
+    const float* mod[kNMod];
+    const void* g[kNCoef];
+    double ratio[kNCoef];
+    double* gm[kNMod];
+    int nx, ny, nz, R, L;
+    long long px, plane;
+    double dt;
+};
+template <class A> cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st);
+
+}  // namespace behf

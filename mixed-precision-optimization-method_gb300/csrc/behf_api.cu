@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "behf_adjoint.cuh"
 #include "behf_aux.cuh"
 #include "behf_internal.cuh"
 #include "behf_medium.cuh"
@@ -121,6 +122,11 @@ struct behf_ctx {
     tiled::VMaps* vmaps = nullptr;
     tiled::TMaps* tmaps = nullptr;
     int* d_err = nullptr;
+    // gradient support: the cell-centred moduli kept on the device (BEHF_OPT_GRADIENT) and the
+    // checkpoint spacing of the gradient's forward pass
+    bool keep_medium = false;
+    float* d_mod[kNMod] = {};
+    int ck_stride = 0;
 
     ~behf_ctx() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -423,6 +429,15 @@ behf_status set_medium_dev(behf_ctx* c, const float* const mod[kNMod]) {
         c->scales[3] = pow2_round(ss);
     }
     CK(cudaMemcpyAsync(c->d_rho, mod[BEHF_RHO], N * 4, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->keep_medium) {
+        for (int q = 0; q < kNMod; q++) {
+            if (!c->d_mod[q]) {
+                behf_status sa = c->dalloc((void**)&c->d_mod[q], (size_t)N * 4);
+                if (sa) return sa;
+            }
+            CK(cudaMemcpyAsync(c->d_mod[q], mod[q], N * 4, cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
     behf_status st = BEHF_OK;
     switch (c->prec) {
         case BEHF_FP64: st = build_coefs<double>(c, mod); break;
@@ -806,6 +821,15 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative chunk");
             c->chunk = value;
             break;
+        case BEHF_OPT_GRADIENT:
+            if (c->medium_set && value && !c->d_mod[0])
+                return fail(BEHF_ERR_STATE, "BEHF_OPT_GRADIENT must be set before the medium");
+            c->keep_medium = value != 0;
+            break;
+        case BEHF_OPT_CHECKPOINT:
+            if (value < 0) return fail(BEHF_ERR_INVALID, "negative checkpoint spacing");
+            c->ck_stride = value;
+            break;
         default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
     }
     c->invalidate_graph();
@@ -918,6 +942,287 @@ behf_status behf_health(behf_ctx* c, double* norms) {
     if (norms) std::memcpy(norms, h, sizeof h);
     if (flag) return fail(BEHF_ERR_NONFINITE, "a field holds NaN/Inf or saturates its storage format");
     return BEHF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// ------------------------------------------------------------------------------------------------ gradient
+// Adjoint-state gradient with sqrt(N) checkpointing.  Forward from rest over nt steps, saving the full state
+// (fields + CPML memory) every ck steps; then per segment, last first: restore, recompute the segment keeping
+// every step's fields after V (and the force source), and run the adjoint steps backwards through it.
+// adj: [nrec][nt] host, dJ/d seismogram (physical units); obs != NULL: adj = seis - obs, J = |adj|^2 / 2.
+struct DevBuf {
+    behf_ctx* c;
+    std::vector<void*> ptrs;
+    explicit DevBuf(behf_ctx* cc) : c(cc) {}
+    ~DevBuf() {
+        for (void* p : ptrs) c->dfree(p);
+    }
+    behf_status get(void** out, size_t bytes) {
+        behf_status st = c->dalloc(out, align256(bytes ? bytes : 1));
+        if (!st) ptrs.push_back(*out);
+        return st;
+    }
+};
+
+template <class S>
+behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const double* obs, double* misfit,
+                          double* gw_host, double* const gm_host[kNMod]) {
+    typedef typename Traits<S>::C A;
+    if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before the gradient");
+    if (!c->keep_medium || !c->d_mod[0])
+        return fail(BEHF_ERR_STATE, "set BEHF_OPT_GRADIENT before the medium to compute gradients");
+    if (!c->src_set) return fail(BEHF_ERR_STATE, "the gradient needs a source");
+    if (nt < 1) return fail(BEHF_ERR_INVALID, "nt must be positive");
+    if (c->nrec < 1 || c->cap < nt) return fail(BEHF_ERR_INVALID, "receivers with capacity >= nt are required");
+    const Geom& g = c->g;
+    const size_t nf = (size_t)c->nfield, asz = sizeof(A);
+    const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
+    const size_t sl[3] = {(size_t)c->grid.nz * c->grid.ny * g.W, (size_t)c->grid.nz * g.W * c->grid.nx,
+                          (size_t)g.W * c->grid.ny * c->grid.nx};
+    const int S_ = c->ck_stride > 0 ? c->ck_stride : std::max(1, (int)std::lround(std::sqrt((double)nt)));
+    const int nseg = (nt + S_ - 1) / S_;
+    DevBuf buf(c);
+    AdjPtrs a{};
+    behf_status st = BEHF_OK;
+    for (int q = 0; q < kNField && !st; q++) st = buf.get(&a.lf[q], nf * asz);
+    for (int q = 0; q < 7 && !st; q++) st = buf.get(&a.tmp[q], nf * asz);
+    for (int q = 0; q < kNCoef && !st; q++) st = buf.get(&a.g[q], nf * asz);
+    if (g.W > 0)
+        for (int ax = 0; ax < 3 && !st; ax++)
+            for (int s = 0; s < 8 && !st; s++) {
+                st = buf.get(&a.lpsi[ax][s], sl[ax] * asz);
+                if (!st) st = buf.get(&a.lprv[ax][s], sl[ax] * asz);
+            }
+    // checkpoint: 13 fields then 48 CPML arrays; snapshot: 13 fields
+    size_t ck_bytes = kNField * align256(nf * c->es);
+    if (g.W > 0)
+        for (int ax = 0; ax < 3; ax++) ck_bytes += 16 * align256(sl[ax] * c->ws);
+    const size_t snap_bytes = kNField * align256(nf * c->es);
+    char* ck = nullptr;
+    char* snap = nullptr;
+    double *d_adj = nullptr, *d_gw = nullptr, *d_gfac = nullptr, *d_gm = nullptr;
+    if (!st) st = buf.get((void**)&ck, ck_bytes * nseg);
+    if (!st) st = buf.get((void**)&snap, snap_bytes * (S_ + 1));
+    if (!st) st = buf.get((void**)&d_adj, (size_t)c->nrec * nt * 8);
+    if (!st) st = buf.get((void**)&d_gw, (size_t)nt * 8);
+    if (!st) st = buf.get((void**)&d_gfac, 8);
+    if (st) return st;
+    for (int q = 0; q < kNField; q++) CK(cudaMemsetAsync(a.lf[q], 0, nf * asz, c->stream));
+    for (int q = 0; q < 7; q++) CK(cudaMemsetAsync(a.tmp[q], 0, nf * asz, c->stream));
+    for (int q = 0; q < kNCoef; q++) CK(cudaMemsetAsync(a.g[q], 0, nf * asz, c->stream));
+    if (g.W > 0)
+        for (int ax = 0; ax < 3; ax++)
+            for (int s = 0; s < 8; s++) {
+                CK(cudaMemsetAsync(a.lpsi[ax][s], 0, sl[ax] * asz, c->stream));
+                CK(cudaMemsetAsync(a.lprv[ax][s], 0, sl[ax] * asz, c->stream));
+            }
+    CK(cudaMemsetAsync(d_gw, 0, (size_t)nt * 8, c->stream));
+    CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
+    a.grad = 1;
+
+    auto copy_state = [&](char* dst, bool save) -> cudaError_t {
+        char* q = dst;
+        for (int f = 0; f < kNField; f++, q += align256(nf * c->es)) {
+            cudaError_t e = save ? cudaMemcpyAsync(q, c->p.f[f], nf * c->es, cudaMemcpyDeviceToDevice, c->stream)
+                                 : cudaMemcpyAsync(c->p.f[f], q, nf * c->es, cudaMemcpyDeviceToDevice, c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        if (g.W > 0)
+            for (int ax = 0; ax < 3; ax++)
+                for (int s = 0; s < 16; s++, q += align256(sl[ax] * c->ws)) {
+                    void* m = s < 8 ? c->p.psi[ax][s] : c->p.prv[ax][s - 8];
+                    cudaError_t e = save ? cudaMemcpyAsync(q, m, sl[ax] * c->ws, cudaMemcpyDeviceToDevice, c->stream)
+                                         : cudaMemcpyAsync(m, q, sl[ax] * c->ws, cudaMemcpyDeviceToDevice, c->stream);
+                    if (e != cudaSuccess) return e;
+                }
+        return cudaSuccess;
+    };
+    auto snap_fields = [&](int idx) -> cudaError_t {
+        char* q = snap + snap_bytes * idx;
+        for (int f = 0; f < kNField; f++, q += align256(nf * c->es)) {
+            cudaError_t e = cudaMemcpyAsync(q, c->p.f[f], nf * c->es, cudaMemcpyDeviceToDevice, c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
+    auto snap_ptr = [&](int idx, int f) -> const void* { return snap + snap_bytes * idx + align256(nf * c->es) * f; };
+
+    // forward pass with checkpoints (seismograms recorded as in behf_run)
+    st = zero_state(c);
+    if (st) return st;
+    for (int sg = 0; sg < nseg; sg++) {
+        const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
+        CK(copy_state(ck + ck_bytes * sg, true));
+        st = behf_run_async(c, s1 - s0);
+        if (st) return st;
+    }
+    st = behf_sync(c);
+    if (st) return st;
+
+    // adjoint source (host): residual and misfit, scaled by alpha so the adjoint state stays O(1)
+    const int nrec = c->nrec;
+    std::vector<double> adj((size_t)nrec * nt);
+    std::vector<int> comp(nrec);
+    CK(cudaMemcpy(comp.data(), c->d_rec_comp, (size_t)nrec * 4, cudaMemcpyDeviceToHost));
+    if (obs) {
+        std::vector<double> seis((size_t)nrec * nt);
+        CK(cudaMemcpy2D(seis.data(), (size_t)nt * 8, c->d_seis, (size_t)c->cap * 8, (size_t)nt * 8, nrec,
+                        cudaMemcpyDeviceToHost));
+        double J = 0;
+        for (size_t i = 0; i < adj.size(); i++) {
+            adj[i] = seis[i] - obs[i];
+            J += 0.5 * adj[i] * adj[i];
+        }
+        if (misfit) *misfit = J;
+    } else {
+        std::memcpy(adj.data(), adj_host, adj.size() * 8);
+    }
+    double amax = 0;
+    for (int r = 0; r < nrec; r++)
+        for (int it = 0; it < nt; it++)
+            amax = std::fmax(amax, std::fabs(adj[(size_t)r * nt + it]) / c->field_scale(comp[r]));
+    const double alpha = amax > 0 ? 1.0 / amax : 1.0;
+    AdjScales sc;
+    for (int q = 0; q < kNField; q++) sc.s[q] = alpha / c->field_scale(q);
+    CK(cudaMemcpy(d_adj, adj.data(), adj.size() * 8, cudaMemcpyHostToDevice));
+
+    double fac = 0;
+    CK(source_factor(c, &fac));
+    const long long so = c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]);
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
+        CK(copy_state(ck + ck_bytes * sg, false));
+        CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        CK(snap_fields(0));
+        for (int it = s0; it < s1; it++) {  // recompute, keeping the fields after V (+ force)
+            if (c->src_kind != BEHF_SRC_FORCE_Z)
+                CK(aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream));
+            CK(dispatch_update(c, true));
+            if (c->src_kind == BEHF_SRC_FORCE_Z)
+                CK(aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream));
+            CK(snap_fields(it - s0 + 1));
+            CK(dispatch_update(c, false));
+            CK(aux_tick(c->d_it, 1, c->stream));
+            c->launches += 4;
+        }
+        for (int it = s1 - 1; it >= s0; it--) {
+            for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(it - s0 + 1, f);
+            for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(it - s0, BEHF_QX + d);
+            CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
+            CK(adj_step_t<S>(g, c->p, a, c->stream));
+            CK(adj_point<S>(a, so, c->src_kind, 0, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
+            CK(adj_step_v<S>(g, c->p, a, c->stream));
+            CK(adj_point<S>(a, so, c->src_kind, 1, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
+            c->launches += g.W > 0 ? 9 : 7;
+        }
+    }
+    CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    st = behf_sync(c);
+    if (st) return st;
+    c->step = nt;
+
+    if (gw_host) {
+        CK(cudaMemcpy(gw_host, d_gw, (size_t)nt * 8, cudaMemcpyDeviceToHost));
+        for (int it = 0; it < nt; it++) gw_host[it] /= alpha;
+    }
+    bool want_mod = false;
+    for (int q = 0; q < kNMod; q++) want_mod = want_mod || gm_host[q];
+    if (!want_mod) return BEHF_OK;
+    if ((st = buf.get((void**)&d_gm, N * 8 * kNMod))) return st;
+    GradModArgs ga{};
+    for (int q = 0; q < kNMod; q++) {
+        ga.mod[q] = c->d_mod[q];
+        ga.gm[q] = d_gm + N * q;
+    }
+    for (int q = 0; q < kNCoef; q++) ga.g[q] = a.g[q];
+    const double sv = c->scales[0], sq = c->scales[1], ss = c->scales[2], sp = c->scales[3];
+    const double hi = 1.0 / c->grid.h;
+    for (int d = 0; d < 3; d++) {
+        ga.ratio[VW1X + d] = 1.0;
+        ga.ratio[VW2X + d] = sq / ss * hi;
+        ga.ratio[VW3X + d] = sq / sp * hi;
+        ga.ratio[VU1X + d] = sv / ss * hi;
+        ga.ratio[VU2X + d] = sv / sq;
+    }
+    ga.ratio[P1] = sp / sv * hi;
+    ga.ratio[P2] = sp / sq * hi;
+    ga.ratio[S1] = ga.ratio[S2] = ss / sv * hi;
+    ga.ratio[S3] = ss / sq * hi;
+    ga.ratio[SXYC] = ga.ratio[SXZC] = ga.ratio[SYZC] = ss / sv * hi;
+    ga.nx = c->grid.nx;
+    ga.ny = c->grid.ny;
+    ga.nz = c->grid.nz;
+    ga.R = g.R;
+    ga.L = g.W > 0 ? g.L : 0;
+    ga.px = g.px;
+    ga.plane = g.plane;
+    ga.dt = c->grid.dt;
+    CK(adj_grad_moduli<A>(ga, c->stream));
+    c->launches++;
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < kNMod; q++) {
+        if (!gm_host[q]) continue;
+        CK(cudaMemcpy(gm_host[q], d_gm + N * q, N * 8, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < N; i++) gm_host[q][i] /= alpha;
+    }
+    if (c->src_kind == BEHF_SRC_FORCE_Z && gm_host[BEHF_RHO]) {
+        // force = dt / rho_z * s_v with rho_z = (rho[src] + rho[src + z]) / 2
+        double gfac = 0;
+        float r[2];
+        const size_t o = ((size_t)c->src_ijk[2] * c->grid.ny + c->src_ijk[1]) * c->grid.nx + c->src_ijk[0];
+        const size_t plane = (size_t)c->grid.nx * c->grid.ny;
+        CK(cudaMemcpy(&gfac, d_gfac, 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&r[0], c->d_mod[BEHF_RHO] + o, 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&r[1], c->d_mod[BEHF_RHO] + o + plane, 4, cudaMemcpyDeviceToHost));
+        const double rz = 0.5 * ((double)r[0] + (double)r[1]);
+        const double gr = gfac / alpha * (-c->grid.dt * c->scales[0] / (rz * rz)) * 0.5;
+        const int n3[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
+        auto inside = [&](int kz) {
+            const int xs[3] = {c->src_ijk[0], c->src_ijk[1], kz};
+            for (int d = 0; d < 3; d++) {
+                const int lo = std::max(ga.L, ga.R) + 1;
+                const int hi3 = ga.L > 0 ? std::min(n3[d] - 2 - ga.L, n3[d] - ga.R - 1) : n3[d] - ga.R - 1;
+                if (xs[d] < lo || xs[d] > hi3) return false;
+            }
+            return true;
+        };
+        if (inside(c->src_ijk[2])) gm_host[BEHF_RHO][o] += gr;
+        if (inside(c->src_ijk[2] + 1)) gm_host[BEHF_RHO][o + plane] += gr;
+    }
+    return BEHF_OK;
+}
+
+behf_status gradient_dispatch(behf_ctx* c, int nt, const double* adj, const double* obs, double* misfit, double* gw,
+                              double* const gm[kNMod]) {
+    double* none[kNMod] = {};
+    double* const* g = gm ? gm : none;
+    switch (c->prec) {
+        case BEHF_FP64: return gradient_impl<double>(c, nt, adj, obs, misfit, gw, g);
+        case BEHF_FP32: return gradient_impl<float>(c, nt, adj, obs, misfit, gw, g);
+        case BEHF_FP16: return gradient_impl<__half>(c, nt, adj, obs, misfit, gw, g);
+        case BEHF_BF16: return gradient_impl<__nv_bfloat16>(c, nt, adj, obs, misfit, gw, g);
+    }
+    return fail(BEHF_ERR_INVALID, "bad precision");
+}
+
+}  // namespace
+
+extern "C" {
+
+behf_status behf_gradient(behf_ctx* c, int nt, const double* adj_src, double* grad_wavelet,
+                          double* const grad_moduli[BEHF_NMOD]) {
+    if (!c || !adj_src) return fail(BEHF_ERR_INVALID, "null argument");
+    return gradient_dispatch(c, nt, adj_src, nullptr, nullptr, grad_wavelet, grad_moduli);
+}
+
+behf_status behf_misfit_gradient(behf_ctx* c, int nt, const double* observed, double* misfit, double* grad_wavelet,
+                                 double* const grad_moduli[BEHF_NMOD]) {
+    if (!c || !observed) return fail(BEHF_ERR_INVALID, "null argument");
+    return gradient_dispatch(c, nt, nullptr, observed, misfit, grad_wavelet, grad_moduli);
 }
 
 }  // extern "C"

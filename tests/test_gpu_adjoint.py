@@ -1,0 +1,138 @@
+"""Adjoint-state gradient on the GPU (behf_gradient / behf_misfit_gradient through the C ABI), against the
+FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identity and finite differences):
+  * FP64: wavelet and moduli gradients within 1e-9 relative L2 of the oracle, every source kind, radius 1/2/4,
+    with and without CPML; dot-product identity within 1e-10; checkpoint spacing changes nothing;
+  * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
+  * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+import behf
+from behf import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def small(n=22, nt=70, R=2, L=4, kind="explosive"):
+    p = P.small64(n=n, nt=nt, radius=R, cpml=L)
+    mod = P.layered((n, n, n), [P.SANDSTONE, P.STIFF], [n // 2 + 2])
+    rng = np.random.default_rng(1)
+    ijk = rng.integers(R + 1, n - R - 1, size=(12, 3)).astype(np.int32)
+    comp = rng.integers(0, 13, size=12).astype(np.int32)
+    return dataclasses.replace(p, mod=mod, src_kind=kind, scales=(1, 1, 1, 1), rec_ijk=ijk, rec_comp=comp)
+
+
+def rel(a, b):
+    d = np.linalg.norm(b.ravel())
+    return np.linalg.norm((a - b).ravel()) / d if d > 0 else np.linalg.norm(a.ravel())
+
+
+def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto"):
+    s = behf.solver_for(p, precision=precision, kernel=kernel, gradient=True, checkpoint=checkpoint)
+    gw, gm = s.gradient(p.nt, adj)
+    seis = s.seismograms()
+    s.close()
+    return seis, gw, gm
+
+
+CASES = [("explosive", 2, 4), ("pressure", 1, 0), ("force_z", 4, 5)]
+
+
+@pytest.mark.parametrize("kind,R,L", CASES)
+def test_gradient_f64_matches_oracle(behf_lib, oracle, kind, R, L):
+    p = small(R=R, L=L, kind=kind)
+    adj = np.random.default_rng(4).standard_normal((len(p.rec_comp), p.nt))
+    ref = oracle.adjoint(p, adj, stride=8)
+    seis, gw, gm = gpu_gradient(p, adj, "f64")
+    assert rel(seis, ref["seis"]) < 1e-10
+    assert rel(gw, ref["grad_wavelet"]) < 1e-9
+    for q in range(9):
+        assert rel(gm[q], ref["grad_mod"][q]) < 1e-8, q
+    assert not gm[:, : max(R, L) + 1].any()  # outside the inverted region
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-10), ("f32", 1e-4)])
+def test_gradient_dot_product(behf_lib, precision, tol):
+    p = small(R=4, L=5, kind="force_z")
+    rng = np.random.default_rng(5)
+    w = rng.standard_normal(p.nt).astype(np.float32)
+    p = dataclasses.replace(p, wavelet=w)
+    s = behf.solver_for(p, precision=precision, gradient=True)
+    s.run(p.nt)
+    d = s.seismograms()
+    r = rng.standard_normal(d.shape)
+    lt, _ = s.gradient(p.nt, r, moduli=False)
+    s.close()
+    lhs, rhs = float((d * r).sum()), float((w.astype(np.float64) * lt).sum())
+    assert abs(lhs - rhs) <= tol * abs(lhs)
+
+
+def test_gradient_checkpoint_spacing(behf_lib):
+    p = small(R=2, L=4)
+    adj = np.random.default_rng(6).standard_normal((len(p.rec_comp), p.nt))
+    _, gw1, gm1 = gpu_gradient(p, adj, "f64", checkpoint=1)
+    _, gw2, gm2 = gpu_gradient(p, adj, "f64", checkpoint=13)
+    _, gw3, gm3 = gpu_gradient(p, adj, "f64", checkpoint=p.nt)
+    for a, b in ((gw1, gw2), (gw1, gw3), (gm1, gm2), (gm1, gm3)):
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("f32", 1e-4), ("f16", 5e-2)])
+def test_gradient_reduced_precision(behf_lib, oracle, precision, tol):
+    p = small(R=4, L=5, kind="explosive")
+    adj = np.random.default_rng(7).standard_normal((len(p.rec_comp), p.nt))
+    ref = oracle.adjoint(p, adj)
+    _, gw, gm = gpu_gradient(p, adj, precision)
+    assert rel(gw, ref["grad_wavelet"]) < tol
+    for q in (0, 2, 5, 6):  # rho, mu, HH, H2U
+        assert rel(gm[q], ref["grad_mod"][q]) < tol, q
+
+
+def test_misfit_gradient_and_finite_differences(behf_lib):
+    p = small(n=24, nt=80, R=2, L=4, kind="explosive")
+    n = p.nx
+    zz, yy, xx = np.meshgrid(*[np.arange(n)] * 3, indexing="ij")
+    blob = np.exp(-((xx - n / 2) ** 2 + (yy - n / 2 - 1) ** 2 + (zz - n / 2 + 1) ** 2) / 6.0)
+    mtrue = p.mod.copy()
+    mtrue[5] *= (1 + 0.05 * blob).astype(np.float32)
+
+    def forward(mod):
+        s = behf.solver_for(dataclasses.replace(p, mod=mod), precision="f64")
+        s.run(p.nt)
+        d = s.seismograms()
+        s.close()
+        return d
+
+    dobs = forward(mtrue)
+    s = behf.solver_for(p, precision="f64", gradient=True)
+    J, gw, gm = s.misfit_gradient(p.nt, dobs)
+    s.close()
+    d0 = forward(p.mod)
+    assert abs(J - 0.5 * ((d0 - dobs) ** 2).sum()) <= 1e-12 * J
+    for q in (0, 5):
+        base = p.mod[q].astype(np.float64)
+        mp, mm = p.mod.copy(), p.mod.copy()
+        mp[q] = (base * (1 + 1e-3 * blob)).astype(np.float32)
+        mm[q] = (base * (1 - 1e-3 * blob)).astype(np.float32)
+        fd = 0.5 * ((forward(mp) - dobs) ** 2).sum() - 0.5 * ((forward(mm) - dobs) ** 2).sum()
+        pred = float((gm[q] * (mp[q].astype(np.float64) - mm[q].astype(np.float64))).sum())
+        assert abs(fd - pred) <= 1e-3 * abs(fd), (q, fd, pred)
+
+
+def test_gradient_errors(behf_lib):
+    p = small()
+    s = behf.solver_for(p, precision="f32")
+    with pytest.raises(behf.BehfError) as e:
+        s.gradient(p.nt, np.zeros((len(p.rec_comp), p.nt)))
+    assert e.value.code == -4  # BEHF_ERR_STATE: gradient support not enabled before the medium
+    with pytest.raises(behf.BehfError):
+        s.enable_gradient()  # too late: the medium is set
+    s.close()
+    s = behf.solver_for(p, precision="f32", gradient=True, capacity=p.nt - 1)
+    with pytest.raises(behf.BehfError):
+        s.gradient(p.nt, np.zeros((len(p.rec_comp), p.nt)))
+    s.close()
