@@ -39,6 +39,12 @@ import numpy as np  # noqa: E402
 METRIC = "Gpt-updates/s (1024^3 FP16 BEHF, seis relL2<=2e-2)"
 UNIT = "Gpt/s"
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the tiled radius-4 FP16
+# kernels on this workload at 1024^3, from one ncu capture (one pass per launch), per updated cell; the
+# bench multiplies by the cells of its own grid.
+NCU_BYTES_PER_CELL = {("f16", "velocity"): 96.42, ("f16", "stress"): 81.66}
+NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1024^3 launch, per cell x cells"
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -53,6 +59,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 comparison run")
     ap.add_argument("--cpu-n", type=int, default=160, help="grid of the CPU sample")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient (adjoint) measurement")
+    ap.add_argument("--adjoint-n", type=int, default=256, help="grid of the gradient measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -198,6 +207,43 @@ def timed_steps(s, steps, world):
     return ms, launches
 
 
+def adjoint_leg(args):
+    """Seconds per shot of the checkpointed adjoint-state gradient (L2 misfit of vz and p) against the same
+    forward run alone, on the inversion workload (256^3, 2000 steps, FP16 storage, FP32 adjoint)."""
+    import torch
+
+    import behf
+    from behf import problems
+    n, nt = args.adjoint_n, args.adjoint_steps
+    s = behf.solver_for(problems.inversion256(n=n, nt=nt, true_model=True), precision=args.precision)
+    s.run(nt)
+    dobs = s.seismograms()
+    s.close()
+    prob = problems.inversion256(n=n, nt=nt, true_model=False)
+    s = behf.solver_for(prob, precision=args.precision, gradient=True)
+    s.run(min(nt, 40))  # warm-up: graph capture, first launches
+    s.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(nt)
+    t1 = time.perf_counter()
+    s.reset()
+    l0 = s.info()["launches"]
+    t2 = time.perf_counter()
+    J, gw, gm = s.misfit_gradient(nt, dobs)
+    t3 = time.perf_counter()
+    launches = s.info()["launches"] - l0
+    s.close()
+    fwd, grad = t1 - t0, t3 - t2
+    return {"workload": f"inversion{n}: {n}^3 two-layer medium, anomaly-free start model, pressure source 25 Hz, "
+                        f"{len(prob.rec_comp)} traces (vz, p), L2 misfit",
+            "steps": nt, "storage": args.precision, "adjoint_arithmetic": "f64" if args.precision == "f64" else "f32",
+            "checkpoint_every": int(round(nt ** 0.5)), "forward_s": fwd, "gradient_s_per_shot": grad,
+            "gradient_over_forward": grad / fwd, "misfit": J, "gpu_launches": int(launches),
+            "grad_norms": {k: float(np.linalg.norm(gm[i])) for i, k in
+                           enumerate(("rho", "rhof", "mu", "M", "C", "HH", "H2U", "C1", "C2"))}}
+
+
 def behf_arm(args, world, rank, local):
     import torch
 
@@ -229,6 +275,9 @@ def behf_arm(args, world, rank, local):
     peak, peak_kind = peak_hbm()
     achieved = ab[dom] * cells / (kt[dom] * 1e-3) / 1e9
     info = s.info()
+    bpc = NCU_BYTES_PER_CELL.get((args.precision, dom)) if info["kernel"] == "tiled" and prob.radius == 4 else None
+    traffic = bpc * cells if bpc is not None else None
+    traffic_src = NCU_SOURCE if bpc is not None else None
 
     # end to end through the C ABI with host buffers: per step, the wavelet sample goes host->device
     # (pinned) and the step's seismogram column (every receiver) comes back device->host (pinned)
@@ -264,6 +313,10 @@ def behf_arm(args, world, rank, local):
             s32.close()
             del s32
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_leg(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, sec = cpu_rate(args.cpu_n, 6, 1)
@@ -276,7 +329,8 @@ def behf_arm(args, world, rank, local):
                "vs_baseline": None, "dtype": args.precision, "data": "synthetic (device-generated random medium)",
                "config": config_dict(args), "e2e": e2e, "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                            "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                            "peak_source": peak_kind,
                             "bytes_per_cell": ab[dom], "kernel_ms": kt[dom]},
                "step_roofline": {"bytes_per_cell_fused": ab["step_fused"], "bytes_per_cell_unfused": ab["step_unfused"],
                                  "achieved": value / world * ab["step_fused"], "frac": value / world * ab["step_fused"] / peak,
@@ -284,7 +338,7 @@ def behf_arm(args, world, rank, local):
                "kernel_ms": kt, "kernel_family": info["kernel"], "scales": info["scales"], "health_ok": ok,
                "fp32": fp32, "fp16_over_fp32": (value / world / fp32["auto"]) if fp32 else None,
                "fp16_over_plain_fp32": (value / world / fp32["plain"]) if fp32 else None,
-               "clocks": clocks, "cpu_baseline": cpu, "device_bytes": info["device_bytes"]}
+               "clocks": clocks, "cpu_baseline": cpu, "device_bytes": info["device_bytes"], "adjoint": adjoint}
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

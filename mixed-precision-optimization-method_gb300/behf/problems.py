@@ -18,6 +18,8 @@ Named workloads (sizes, steps and media of the benchmark and parity cases):
     random1024    1024^3, 3000 steps, 20-cell CPML, sandstone with 5 % Gaussian-correlated (50 m)
                   perturbations of K_dry, mu, phi and log-normal kappa (sigma 0.5), vertical force
                   source, 20 Hz, 512 x 512 surface receivers (vz and p)
+    inversion256  the gradient workload: layered256's medium (+ a 100 m Gaussian anomaly for the true model),
+                  16 pressure-source shots at 25 Hz, 2000 steps, 16 x 16 surface receivers (vz and p)
     borehole      the reference's own problem: 240 x 240 x 360 cells of 1 cm (180^2 x 300 + 30-cell
                   CPML), fluid borehole in a porous formation, 10 kHz, 3500 steps of 1 us, radius 1,
                   txx recorded on the vertical line through the source (main.cpp:20-23, 84-99)
@@ -266,6 +268,26 @@ def layered256(n=256, nt=2000, radius=4, cpml=20, nrec_side=16) -> Problem:
                    cpml_v0=p_velocity(STIFF), f0=f0, name=f"layered{n}")
 
 
+def inversion256(n=256, nt=2000, shot=0, true_model=True, radius=4, cpml=20, nrec_side=16) -> Problem:
+    """The gradient workload: the two-layer 256^3 medium of layered256 (interface at z = 640 m), for the true
+    model with a Gaussian anomaly of 100 m radius (K_dry -10 %, kappa x10) above the interface; 25 Hz
+    pressure source of shot `shot` (one of 16 on a 4 x 4 grid at depth L + 6), 16 x 16 surface receivers
+    recording vz and p.  The medium is left to the device generator (extra["spec"])."""
+    h, dt, f0 = 5.0, 4e-4, 25.0
+    zi = n // 2
+    anomaly = dict(center=(n / 2, n / 2, 0.78 * zi), radius=100.0 / h, dkdry=-0.10, kappa_factor=10.0)
+    spec = dict(layers=[SANDSTONE, STIFF], interfaces=(zi,), seed=1234, corr_cells=10.0, pct=0.0,
+                log_kappa_sigma=0.0, anomaly=anomaly if true_model else None)
+    ax = np.linspace(cpml + 4, n - cpml - 5, nrec_side).round().astype(int)
+    X, Y = np.meshgrid(ax, ax, indexing="xy")
+    ijk, comp = line_receivers(X.ravel(), Y.ravel(), cpml + 2, [2, 12])
+    grid = np.linspace(cpml + 10, n - cpml - 11, 4).round().astype(int)
+    src = (int(grid[shot % 4]), int(grid[(shot // 4) % 4]), cpml + 6)
+    return Problem(n, n, n, h, dt, radius, np.zeros((9, 1, 1, 1), np.float32), ricker(nt, dt, f0), src, ijk, comp,
+                   src_kind="pressure", cpml_width=cpml, cpml_v0=p_velocity(STIFF), f0=f0,
+                   name=f"inversion{n}", extra={"spec": spec, "shot": shot})
+
+
 def random1024(n=1024, nt=3000, radius=4, cpml=20, nrec_side=512, seed=1234, medium=True) -> Problem:
     """The 1024^3 random medium; with medium=False the moduli are left for the device generator."""
     h, dt, f0 = 5.0, 4e-4, 20.0
@@ -321,4 +343,5 @@ def borehole(scale: float = 1.0, nt=3500) -> Problem:
                    scales=(1e8, 1e8, 1.0, 1.0), name="borehole")
 
 
-WORKLOADS = {"small64": small64, "layered256": layered256, "random1024": random1024, "borehole": borehole}
+WORKLOADS = {"small64": small64, "layered256": layered256, "random1024": random1024, "borehole": borehole,
+             "inversion256": inversion256}

@@ -12,6 +12,8 @@
 //   CPML (forward  psi' = A psi + B (A prev + D), prev' = D, D~ = D + psi'):
 //        lD = lD~ + B (lpsi + lD~) + lprev;  then  lpsi = A (lpsi + lD~),  lprev = A B (lpsi_old + lD~).
 //   A forward difference's transpose is minus the backward difference of the adjoint and vice versa.
+#include <algorithm>
+
 #include "behf_adjoint.cuh"
 
 namespace behf {
@@ -60,46 +62,6 @@ struct Adj {
     }
     static __device__ __forceinline__ A prof(const void* v, int i) { return reinterpret_cast<const A*>(v)[i]; }
 
-    // derivative-group adjoint t at cell (i,j,k) with the adjoint CPML correction of `slot` on axis ax
-    static __device__ __forceinline__ A lmod(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int t, int ax,
-                                             int slot, bool half, int i, int j, int k) {
-        A v = reinterpret_cast<const A*>(a.tmp[t])[(long long)k * g.plane + (long long)j * g.px + i];
-        if (g.W > 0) {
-            const int pos = ax == 0 ? i : ax == 1 ? j : k;
-            const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
-            if (s >= 0) {
-                const long long so = slab_off(g, ax, i, j, k, s);
-                const A B = half ? prof(p.pb2[ax], pos) : prof(p.pb[ax], pos);
-                v += B * (reinterpret_cast<const A*>(a.lpsi[ax][slot])[so] + v) +
-                     reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
-            }
-        }
-        return v;
-    }
-    // transposed stencils of a corrected derivative-group adjoint along axis ax, at cell (i,j,k):
-    //   fwdL = sum_m w_m (L[+m] - L[-m+1]),  bwdL = sum_m w_m (L[+m-1] - L[-m])
-    static __device__ __forceinline__ A fwdL(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int t, int ax,
-                                             int slot, bool half, int i, int j, int k) {
-        const int di = ax == 0, dj = ax == 1, dk = ax == 2;
-        A acc = 0;
-#pragma unroll
-        for (int m = 1; m <= R; m++)
-            acc += (A)stencil_w<R>(m) * (lmod(g, p, a, t, ax, slot, half, i + m * di, j + m * dj, k + m * dk) -
-                                         lmod(g, p, a, t, ax, slot, half, i - (m - 1) * di, j - (m - 1) * dj,
-                                              k - (m - 1) * dk));
-        return acc;
-    }
-    static __device__ __forceinline__ A bwdL(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int t, int ax,
-                                             int slot, bool half, int i, int j, int k) {
-        const int di = ax == 0, dj = ax == 1, dk = ax == 2;
-        A acc = 0;
-#pragma unroll
-        for (int m = 1; m <= R; m++)
-            acc += (A)stencil_w<R>(m) * (lmod(g, p, a, t, ax, slot, half, i + (m - 1) * di, j + (m - 1) * dj,
-                                              k + (m - 1) * dk) -
-                                         lmod(g, p, a, t, ax, slot, half, i - m * di, j - m * dj, k - m * dk));
-        return acc;
-    }
     // adjoint CPML memory update of one slot
     static __device__ __forceinline__ void lmem(const Geom& g, const DevPtrs& p, const AdjPtrs& a, A lD, int ax,
                                                 int slot, bool half, int pos, long long so) {
@@ -123,9 +85,18 @@ struct Adj {
     (void)sy;                                                           \
     (void)sz;
 
-// ------------------------------------------------------------------------------------------- T^T
+// ------------------------------------------------------------------------------------------- step^T
+// Per backward step: record^T (separate, atomic), then
+//   k_adj_a  T^T per cell: derivative-group adjoints tmpT[7] (0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz) and
+//            the T-coefficient gradients;
+//   k_gather<.., 0>  the T^T gather into lv, lq, the V-slot adjoint memory update of the previous backward
+//            step (from its tmpV at this cell), then V^T per cell: tmpV[6] (0..2 Sigma_x,y,z, 3..5 Dp_x,y,z)
+//            and the V-coefficient gradients;
+//   k_gather<.., 1>  the V^T gather into ls, lp and the T-slot adjoint memory update of this step.
+// A gather reads the adjoint memory of its own slots only, and each memory update runs after every gather
+// that reads those slots.
 template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_t1(Geom g, DevPtrs p, AdjPtrs a) {
+__global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
     typedef Adj<S, R> Q;
     typedef typename Q::A A;
     CELL_INDEX
@@ -134,13 +105,13 @@ __global__ void __launch_bounds__(256) k_adj_t1(Geom g, DevPtrs p, AdjPtrs a) {
     const A lyz = Q::ad(a.lf[BEHF_SYZ])[c];
     const A p1 = Q::coef(g, p, P1, c), p2 = Q::coef(g, p, P2, c);
     const A s1 = Q::coef(g, p, S1, c), s2 = Q::coef(g, p, S2, c), s3 = Q::coef(g, p, S3, c);
-    Q::ad(a.tmp[0])[c] = -p1 * lp + s2 * lxx + s1 * (lyy + lzz);
-    Q::ad(a.tmp[1])[c] = -p1 * lp + s2 * lyy + s1 * (lxx + lzz);
-    Q::ad(a.tmp[2])[c] = -p1 * lp + s2 * lzz + s1 * (lxx + lyy);
-    Q::ad(a.tmp[3])[c] = -p2 * lp + s3 * (lxx + lyy + lzz);
-    Q::ad(a.tmp[4])[c] = Q::coef(g, p, SXYC, c) * lxy;
-    Q::ad(a.tmp[5])[c] = Q::coef(g, p, SXZC, c) * lxz;
-    Q::ad(a.tmp[6])[c] = Q::coef(g, p, SYZC, c) * lyz;
+    Q::ad(a.tmpT[0])[c] = -p1 * lp + s2 * lxx + s1 * (lyy + lzz);
+    Q::ad(a.tmpT[1])[c] = -p1 * lp + s2 * lyy + s1 * (lxx + lzz);
+    Q::ad(a.tmpT[2])[c] = -p1 * lp + s2 * lzz + s1 * (lxx + lyy);
+    Q::ad(a.tmpT[3])[c] = -p2 * lp + s3 * (lxx + lyy + lzz);
+    Q::ad(a.tmpT[4])[c] = Q::coef(g, p, SXYC, c) * lxy;
+    Q::ad(a.tmpT[5])[c] = Q::coef(g, p, SXZC, c) * lxz;
+    Q::ad(a.tmpT[6])[c] = Q::coef(g, p, SYZC, c) * lyz;
     if (a.grad && interior(g, i, j, k)) {
         const A uxx = Q::bwd(a.cur[BEHF_VX], c, 1), uyy = Q::bwd(a.cur[BEHF_VY], c, sy);
         const A uzz = Q::bwd(a.cur[BEHF_VZ], c, sz);
@@ -159,145 +130,218 @@ __global__ void __launch_bounds__(256) k_adj_t1(Geom g, DevPtrs p, AdjPtrs a) {
     }
 }
 
-// groups: 0 uxx, 1 uyy, 2 uzz, 3 w (all three flux divergences), 4 xy, 5 xz, 6 yz
-template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_t2(Geom g, DevPtrs p, AdjPtrs a) {
-    typedef Adj<S, R> Q;
-    typedef typename Q::A A;
-    CELL_INDEX
-    // forward: uxx = bwd_x vx (x slot 4), uxy = fwd_y vx (y slot 6, half), uxz = fwd_z vx (z slot 6, half), ...
-    Q::ad(a.lf[BEHF_VX])[c] -= Q::fwdL(g, p, a, 0, 0, 4, false, i, j, k) + Q::bwdL(g, p, a, 4, 1, 6, true, i, j, k) +
-                               Q::bwdL(g, p, a, 5, 2, 6, true, i, j, k);
-    Q::ad(a.lf[BEHF_VY])[c] -= Q::fwdL(g, p, a, 1, 1, 4, false, i, j, k) + Q::bwdL(g, p, a, 4, 0, 6, true, i, j, k) +
-                               Q::bwdL(g, p, a, 6, 2, 7, true, i, j, k);
-    Q::ad(a.lf[BEHF_VZ])[c] -= Q::fwdL(g, p, a, 2, 2, 4, false, i, j, k) + Q::bwdL(g, p, a, 5, 0, 7, true, i, j, k) +
-                               Q::bwdL(g, p, a, 6, 1, 7, true, i, j, k);
-    Q::ad(a.lf[BEHF_QX])[c] -= Q::fwdL(g, p, a, 3, 0, 5, false, i, j, k);
-    Q::ad(a.lf[BEHF_QY])[c] -= Q::fwdL(g, p, a, 3, 1, 5, false, i, j, k);
-    Q::ad(a.lf[BEHF_QZ])[c] -= Q::fwdL(g, p, a, 3, 2, 5, false, i, j, k);
-}
+// Gathers, z-marching: a 32 x 8 block owns an xy tile and walks a z range.  Each gather needs 12 corrected
+// derivative-group adjoints: 4 with x stencils (staged per plane in shared memory with an x halo of R), 4 with
+// y stencils (shared memory, y halo R) and 4 with z stencils (a register queue of 2R+1 planes per thread).
+// "Corrected" = the adjoint CPML correction of the stencil's own axis and slot applied at the cell it was read
+// from: lD = lD~ + B (lpsi + lD~) + lprev on slab cells, lD~ elsewhere (zero off the updated cells).
+constexpr int GX = 32, GY = 8;
+
+struct StageSet {
+    const void* arr[3][4];  // [axis][k]
+    int slot[3][4];
+    int half[3][4];
+};
 
 template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_t3(Geom g, DevPtrs p, AdjPtrs a) {
-    typedef Adj<S, R> Q;
-    typedef typename Q::A A;
-    CELL_INDEX
-    const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
-    if (si < 0 && sj < 0 && sk < 0) return;
-    A t[7];
-#pragma unroll
-    for (int q = 0; q < 7; q++) t[q] = Q::ad(a.tmp[q])[c];
-    if (si >= 0) {
-        const long long so = slab_off(g, 0, i, j, k, si);
-        Q::lmem(g, p, a, t[0], 0, 4, false, i, so);
-        Q::lmem(g, p, a, t[3], 0, 5, false, i, so);
-        Q::lmem(g, p, a, t[4], 0, 6, true, i, so);
-        Q::lmem(g, p, a, t[5], 0, 7, true, i, so);
-    }
-    if (sj >= 0) {
-        const long long so = slab_off(g, 1, i, j, k, sj);
-        Q::lmem(g, p, a, t[1], 1, 4, false, j, so);
-        Q::lmem(g, p, a, t[3], 1, 5, false, j, so);
-        Q::lmem(g, p, a, t[4], 1, 6, true, j, so);
-        Q::lmem(g, p, a, t[6], 1, 7, true, j, so);
-    }
-    if (sk >= 0) {
-        const long long so = slab_off(g, 2, i, j, k, sk);
-        Q::lmem(g, p, a, t[2], 2, 4, false, k, so);
-        Q::lmem(g, p, a, t[3], 2, 5, false, k, so);
-        Q::lmem(g, p, a, t[5], 2, 6, true, k, so);
-        Q::lmem(g, p, a, t[6], 2, 7, true, k, so);
-    }
-}
-
-// ------------------------------------------------------------------------------------------- V^T
-// groups: 0..2 Sigma_x, Sigma_y, Sigma_z;  3..5 Dp_x, Dp_y, Dp_z
-template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_v1(Geom g, DevPtrs p, AdjPtrs a) {
-    typedef Adj<S, R> Q;
-    typedef typename Q::A A;
-    CELL_INDEX
-    const bool gr = a.grad && interior(g, i, j, k);
-    A sum[3] = {0, 0, 0}, dp[3] = {0, 0, 0};
-    if (gr) {
-        sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) + Q::bwd(a.cur[BEHF_SXZ], c, sz);
-        sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sz);
-        sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sy);
-        dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
-        dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
-        dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
-    }
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const int vw3 = (d == 2 && g.bug) ? VW3Y : VW3X + d;
-        A* lvp = Q::ad(a.lf[BEHF_VX + d]) + c;
-        A* lqp = Q::ad(a.lf[BEHF_QX + d]) + c;
-        const A lv = *lvp, lq = *lqp;
-        const A vu2 = Q::coef(g, p, VU2X + d, c);
-        const A mu = lq - vu2 * lv;
-        *lqp = Q::vw1(p, d, c) * mu + vu2 * lv;
-        Q::ad(a.tmp[d])[c] = Q::coef(g, p, VU1X + d, c) * lv - Q::coef(g, p, VW2X + d, c) * mu;
-        Q::ad(a.tmp[3 + d])[c] = -Q::coef(g, p, vw3, c) * mu;
-        if (gr) {
-            const A qo = Q::ls(a.qprev[d], c), qn = Q::ls(a.cur[BEHF_QX + d], c);
-            Q::ad(a.g[VW1X + d])[c] += mu * qo;
-            Q::ad(a.g[VW2X + d])[c] += -mu * sum[d];
-            Q::ad(a.g[vw3])[c] += -mu * dp[d];
-            Q::ad(a.g[VU1X + d])[c] += lv * sum[d];
-            Q::ad(a.g[VU2X + d])[c] += -lv * (qn - qo);
+struct G25 {
+    typedef typename Traits<S>::C A;
+    static constexpr int XW = GX + 2 * R;
+    static constexpr int YH = GY + 2 * R;
+    static __device__ __forceinline__ A corr(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const void* arr,
+                                             int ax, int slot, int half, int x, int y, int k) {
+        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) return (A)0;
+        A v = reinterpret_cast<const A*>(arr)[(long long)k * g.plane + (long long)y * g.px + x];
+        if (g.W > 0) {
+            const int pos = ax == 0 ? x : ax == 1 ? y : k;
+            const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
+            if (s >= 0) {
+                const long long so = slab_off(g, ax, x, y, k, s);
+                const A B = reinterpret_cast<const A*>(half ? p.pb2[ax] : p.pb[ax])[pos];
+                v += B * (reinterpret_cast<const A*>(a.lpsi[ax][slot])[so] + v) +
+                     reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
+            }
         }
+        return v;
     }
-}
-
-template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_v2(Geom g, DevPtrs p, AdjPtrs a) {
-    typedef Adj<S, R> Q;
-    typedef typename Q::A A;
-    CELL_INDEX
-    // forward: x1 = fwd_x sxx (x slot 0, half), x2 = bwd_y sxy (y slot 2), x3 = bwd_z sxz (z slot 2),
-    //          y1 = fwd_y syy (y slot 0, half), y2 = bwd_x sxy (x slot 2), y3 = bwd_z syz (z slot 3),
-    //          z1 = fwd_z szz (z slot 0, half), z2 = bwd_x sxz (x slot 3), z3 = bwd_y syz (y slot 3),
-    //          s1..s3 = fwd p (slot 1, half)
-    Q::ad(a.lf[BEHF_SXX])[c] -= Q::bwdL(g, p, a, 0, 0, 0, true, i, j, k);
-    Q::ad(a.lf[BEHF_SYY])[c] -= Q::bwdL(g, p, a, 1, 1, 0, true, i, j, k);
-    Q::ad(a.lf[BEHF_SZZ])[c] -= Q::bwdL(g, p, a, 2, 2, 0, true, i, j, k);
-    Q::ad(a.lf[BEHF_SXY])[c] -= Q::fwdL(g, p, a, 0, 1, 2, false, i, j, k) + Q::fwdL(g, p, a, 1, 0, 2, false, i, j, k);
-    Q::ad(a.lf[BEHF_SXZ])[c] -= Q::fwdL(g, p, a, 0, 2, 2, false, i, j, k) + Q::fwdL(g, p, a, 2, 0, 3, false, i, j, k);
-    Q::ad(a.lf[BEHF_SYZ])[c] -= Q::fwdL(g, p, a, 1, 2, 3, false, i, j, k) + Q::fwdL(g, p, a, 2, 1, 3, false, i, j, k);
-    Q::ad(a.lf[BEHF_P])[c] -= Q::bwdL(g, p, a, 3, 0, 1, true, i, j, k) + Q::bwdL(g, p, a, 4, 1, 1, true, i, j, k) +
-                              Q::bwdL(g, p, a, 5, 2, 1, true, i, j, k);
-}
-
-template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_v3(Geom g, DevPtrs p, AdjPtrs a) {
-    typedef Adj<S, R> Q;
-    typedef typename Q::A A;
-    CELL_INDEX
-    const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
-    if (si < 0 && sj < 0 && sk < 0) return;
-    A t[6];
+    // w[d + R] = L[c + d]:  fwdL = sum_m w_m (L[+m] - L[1-m]),  bwdL = sum_m w_m (L[m-1] - L[-m])
+    template <class F>
+    static __device__ __forceinline__ A fwd(F w) {
+        A acc = 0;
 #pragma unroll
-    for (int q = 0; q < 6; q++) t[q] = Q::ad(a.tmp[q])[c];
-    if (si >= 0) {
-        const long long so = slab_off(g, 0, i, j, k, si);
-        Q::lmem(g, p, a, t[0], 0, 0, true, i, so);
-        Q::lmem(g, p, a, t[3], 0, 1, true, i, so);
-        Q::lmem(g, p, a, t[1], 0, 2, false, i, so);
-        Q::lmem(g, p, a, t[2], 0, 3, false, i, so);
+        for (int m = 1; m <= R; m++) acc += (A)stencil_w<R>(m) * (w(m) - w(1 - m));
+        return acc;
     }
-    if (sj >= 0) {
-        const long long so = slab_off(g, 1, i, j, k, sj);
-        Q::lmem(g, p, a, t[1], 1, 0, true, j, so);
-        Q::lmem(g, p, a, t[4], 1, 1, true, j, so);
-        Q::lmem(g, p, a, t[0], 1, 2, false, j, so);
-        Q::lmem(g, p, a, t[2], 1, 3, false, j, so);
+    template <class F>
+    static __device__ __forceinline__ A bwd(F w) {
+        A acc = 0;
+#pragma unroll
+        for (int m = 1; m <= R; m++) acc += (A)stencil_w<R>(m) * (w(m - 1) - w(-m));
+        return acc;
     }
-    if (sk >= 0) {
-        const long long so = slab_off(g, 2, i, j, k, sk);
-        Q::lmem(g, p, a, t[2], 2, 0, true, k, so);
-        Q::lmem(g, p, a, t[5], 2, 1, true, k, so);
-        Q::lmem(g, p, a, t[0], 2, 2, false, k, so);
-        Q::lmem(g, p, a, t[1], 2, 3, false, k, so);
+};
+
+// KIND 0: T^T gather (X: T0 s4, T4 s6h, T5 s7h, T3 s5;  Y: T1 s4, T4 s6h, T6 s7h, T3 s5;
+//                      Z: T2 s4, T5 s6h, T6 s7h, T3 s5), then V^T per cell.
+// KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
+//                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update.
+template <class S, int R, int KIND>
+__global__ void __launch_bounds__(256) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc, int first) {
+    typedef G25<S, R> W;
+    typedef Adj<S, R> Q;
+    typedef typename W::A A;
+    __shared__ A shx[4][GY][W::XW];
+    __shared__ A shy[4][W::YH][GX];
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * GX + tx;
+    const int i0 = R + blockIdx.x * GX, j0 = R + blockIdx.y * GY;
+    const int i = i0 + tx, j = j0 + ty;
+    const bool valid = i < g.nx - R && j < g.ny - R;
+    const int kb = R + blockIdx.z * zc, ke = min(kb + zc, g.nz - R);
+    if (kb >= ke) return;
+    A zq[4][2 * R + 1];
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int d = 0; d < 2 * R; d++)
+                zq[q][d] = W::corr(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, kb - R + d);
+    }
+    const long long sy = g.px, sz = g.plane;
+    for (int k = kb; k < ke; k++) {
+        for (int e = t; e < 4 * GY * W::XW; e += GX * GY) {
+            const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
+            shx[q][r][cc] = W::corr(g, p, a, ss.arr[0][q], 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
+        }
+        for (int e = t; e < 4 * W::YH * GX; e += GX * GY) {
+            const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
+            shy[q][r][cc] = W::corr(g, p, a, ss.arr[1][q], 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
+        }
+        if (valid) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                zq[q][2 * R] = W::corr(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, k + R);
+        }
+        __syncthreads();
+        if (valid) {
+            const long long c = k * sz + j * sy + i;
+#define WX(q) [&](int d) { return shx[q][ty][tx + R + d]; }
+#define WY(q) [&](int d) { return shy[q][ty + R + d][tx]; }
+#define WZ(q) [&](int d) { return zq[q][R + d]; }
+            if (KIND == 0) {
+                A dl[6];
+                dl[0] = W::fwd(WX(0)) + W::bwd(WY(1)) + W::bwd(WZ(1));
+                dl[1] = W::fwd(WY(0)) + W::bwd(WX(1)) + W::bwd(WZ(2));
+                dl[2] = W::fwd(WZ(0)) + W::bwd(WX(2)) + W::bwd(WY(2));
+                dl[3] = W::fwd(WX(3));
+                dl[4] = W::fwd(WY(3));
+                dl[5] = W::fwd(WZ(3));
+                const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
+                if (!first && g.W > 0 && (si >= 0 || sj >= 0 || sk >= 0)) {  // V-slot memory of the previous step
+                    A tv[6];
+#pragma unroll
+                    for (int q = 0; q < 6; q++) tv[q] = Q::ad(a.tmpV[q])[c];
+                    if (si >= 0) {
+                        const long long so = slab_off(g, 0, i, j, k, si);
+                        Q::lmem(g, p, a, tv[0], 0, 0, true, i, so);
+                        Q::lmem(g, p, a, tv[3], 0, 1, true, i, so);
+                        Q::lmem(g, p, a, tv[1], 0, 2, false, i, so);
+                        Q::lmem(g, p, a, tv[2], 0, 3, false, i, so);
+                    }
+                    if (sj >= 0) {
+                        const long long so = slab_off(g, 1, i, j, k, sj);
+                        Q::lmem(g, p, a, tv[1], 1, 0, true, j, so);
+                        Q::lmem(g, p, a, tv[4], 1, 1, true, j, so);
+                        Q::lmem(g, p, a, tv[0], 1, 2, false, j, so);
+                        Q::lmem(g, p, a, tv[2], 1, 3, false, j, so);
+                    }
+                    if (sk >= 0) {
+                        const long long so = slab_off(g, 2, i, j, k, sk);
+                        Q::lmem(g, p, a, tv[2], 2, 0, true, k, so);
+                        Q::lmem(g, p, a, tv[5], 2, 1, true, k, so);
+                        Q::lmem(g, p, a, tv[0], 2, 2, false, k, so);
+                        Q::lmem(g, p, a, tv[1], 2, 3, false, k, so);
+                    }
+                }
+                // V^T at this cell with lv = lv_old - dl[0..2], lq' = lq_old - dl[3..5]
+                const bool gr = a.grad && interior(g, i, j, k);
+                A sum[3] = {0, 0, 0}, dp[3] = {0, 0, 0};
+                if (gr) {
+                    sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) + Q::bwd(a.cur[BEHF_SXZ], c, sz);
+                    sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sz);
+                    sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sy);
+                    dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
+                    dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
+                    dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const int vw3 = (d == 2 && g.bug) ? VW3Y : VW3X + d;
+                    A* lvp = Q::ad(a.lf[BEHF_VX + d]) + c;
+                    A* lqp = Q::ad(a.lf[BEHF_QX + d]) + c;
+                    const A lv = *lvp - dl[d], lq = *lqp - dl[3 + d];
+                    const A vu2 = Q::coef(g, p, VU2X + d, c);
+                    const A mu = lq - vu2 * lv;
+                    *lvp = lv;
+                    *lqp = Q::vw1(p, d, c) * mu + vu2 * lv;
+                    Q::ad(a.tmpV[d])[c] = Q::coef(g, p, VU1X + d, c) * lv - Q::coef(g, p, VW2X + d, c) * mu;
+                    Q::ad(a.tmpV[3 + d])[c] = -Q::coef(g, p, vw3, c) * mu;
+                    if (gr) {
+                        const A qo = Q::ls(a.qprev[d], c), qn = Q::ls(a.cur[BEHF_QX + d], c);
+                        Q::ad(a.g[VW1X + d])[c] += mu * qo;
+                        Q::ad(a.g[VW2X + d])[c] += -mu * sum[d];
+                        Q::ad(a.g[vw3])[c] += -mu * dp[d];
+                        Q::ad(a.g[VU1X + d])[c] += lv * sum[d];
+                        Q::ad(a.g[VU2X + d])[c] += -lv * (qn - qo);
+                    }
+                }
+            } else {
+                Q::ad(a.lf[BEHF_SXX])[c] -= W::bwd(WX(0));
+                Q::ad(a.lf[BEHF_SYY])[c] -= W::bwd(WY(0));
+                Q::ad(a.lf[BEHF_SZZ])[c] -= W::bwd(WZ(0));
+                Q::ad(a.lf[BEHF_SXY])[c] -= W::fwd(WY(1)) + W::fwd(WX(1));
+                Q::ad(a.lf[BEHF_SXZ])[c] -= W::fwd(WZ(1)) + W::fwd(WX(2));
+                Q::ad(a.lf[BEHF_SYZ])[c] -= W::fwd(WZ(2)) + W::fwd(WY(2));
+                Q::ad(a.lf[BEHF_P])[c] -= W::bwd(WX(3)) + W::bwd(WY(3)) + W::bwd(WZ(3));
+                // T-slot adjoint memory of this step (its gathers ran in the KIND 0 launch)
+                const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
+                if (g.W > 0 && (si >= 0 || sj >= 0 || sk >= 0)) {
+                    A tt[7];
+#pragma unroll
+                    for (int q = 0; q < 7; q++) tt[q] = Q::ad(a.tmpT[q])[c];
+                    if (si >= 0) {
+                        const long long so = slab_off(g, 0, i, j, k, si);
+                        Q::lmem(g, p, a, tt[0], 0, 4, false, i, so);
+                        Q::lmem(g, p, a, tt[3], 0, 5, false, i, so);
+                        Q::lmem(g, p, a, tt[4], 0, 6, true, i, so);
+                        Q::lmem(g, p, a, tt[5], 0, 7, true, i, so);
+                    }
+                    if (sj >= 0) {
+                        const long long so = slab_off(g, 1, i, j, k, sj);
+                        Q::lmem(g, p, a, tt[1], 1, 4, false, j, so);
+                        Q::lmem(g, p, a, tt[3], 1, 5, false, j, so);
+                        Q::lmem(g, p, a, tt[4], 1, 6, true, j, so);
+                        Q::lmem(g, p, a, tt[6], 1, 7, true, j, so);
+                    }
+                    if (sk >= 0) {
+                        const long long so = slab_off(g, 2, i, j, k, sk);
+                        Q::lmem(g, p, a, tt[2], 2, 4, false, k, so);
+                        Q::lmem(g, p, a, tt[3], 2, 5, false, k, so);
+                        Q::lmem(g, p, a, tt[5], 2, 6, true, k, so);
+                        Q::lmem(g, p, a, tt[6], 2, 7, true, k, so);
+                    }
+                }
+            }
+#undef WX
+#undef WY
+#undef WZ
+        }
+        __syncthreads();
+        if (valid) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int d = 0; d < 2 * R; d++) zq[q][d] = zq[q][d + 1];
+        }
     }
 }
 
@@ -314,17 +358,17 @@ __global__ void k_adj_record(AdjPtrs a, const long long* off, const int* comp, i
 }
 
 template <class A>
-__global__ void k_adj_point(AdjPtrs a, long long o, int kind, int phase, double fac, const float* w, int nw, int it,
-                            double* gw, double* gfac) {
+__global__ void k_adj_point(AdjPtrs a, long long o, int kind, double fac, const float* w, int nw, int it, double* gw,
+                            double* gfac) {
     auto L = [&](int q) { return (double)reinterpret_cast<const A*>(a.lf[q])[o]; };
-    if (phase == 0) {
-        if (kind != BEHF_SRC_FORCE_Z) return;
+    if (kind == BEHF_SRC_FORCE_Z) {  // injected into vz between V and T; V^T leaves lv unchanged
         const double lvz = L(BEHF_VZ);
         gw[it] = fac * lvz;
         if (it < nw) *gfac += (double)w[it] * lvz;  // samples past the wavelet are not injected
+    } else if (kind == BEHF_SRC_EXPLOSIVE) {
+        gw[it] = fac * (L(BEHF_SXX) + L(BEHF_SYY) + L(BEHF_SZZ));
     } else {
-        if (kind == BEHF_SRC_EXPLOSIVE) gw[it] = fac * (L(BEHF_SXX) + L(BEHF_SYY) + L(BEHF_SZZ));
-        else if (kind == BEHF_SRC_PRESSURE) gw[it] = fac * L(BEHF_P);
+        gw[it] = fac * L(BEHF_P);
     }
 }
 
@@ -423,43 +467,55 @@ __global__ void k_grad_moduli(GradModArgs a) {
 }
 
 template <class S, int R>
-cudaError_t adj_t_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
+cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st) {
     const dim3 block(32, 8, 1);
-    const dim3 grid((g.nx - 2 * R + 31) / 32, (g.ny - 2 * R + 7) / 8, g.nz - 2 * R);
-    k_adj_t1<S, R><<<grid, block, 0, st>>>(g, p, a);
-    k_adj_t2<S, R><<<grid, block, 0, st>>>(g, p, a);
-    if (g.W > 0) k_adj_t3<S, R><<<grid, block, 0, st>>>(g, p, a);
-    return cudaGetLastError();
-}
-template <class S, int R>
-cudaError_t adj_v_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
-    const dim3 block(32, 8, 1);
-    const dim3 grid((g.nx - 2 * R + 31) / 32, (g.ny - 2 * R + 7) / 8, g.nz - 2 * R);
-    k_adj_v1<S, R><<<grid, block, 0, st>>>(g, p, a);
-    k_adj_v2<S, R><<<grid, block, 0, st>>>(g, p, a);
-    if (g.W > 0) k_adj_v3<S, R><<<grid, block, 0, st>>>(g, p, a);
+    const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
+    const dim3 grid((nxu + 31) / 32, (nyu + 7) / 8, nzu);
+    k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a);
+    // gathers: z chunks so that about four CTAs per SM are resident
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 132;
+    }
+    const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
+    int nch = (4 * sms + nxy - 1) / nxy;
+    nch = std::max(1, std::min(nch, std::max(1, nzu / 8)));
+    const int zc = (nzu + nch - 1) / nch;
+    const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);
+    StageSet t{}, v{};
+    // T^T gather: x {T0 s4, T4 s6h, T5 s7h, T3 s5}, y {T1 s4, T4 s6h, T6 s7h, T3 s5}, z {T2 s4, T5 s6h, T6 s7h, T3 s5}
+    const int tq[3][4] = {{0, 4, 5, 3}, {1, 4, 6, 3}, {2, 5, 6, 3}};
+    const int ts[4] = {4, 6, 7, 5}, th[4] = {0, 1, 1, 0};
+    const int tz_s[4] = {4, 6, 7, 5};
+    // V^T gather: x {V0 s0h, V1 s2, V2 s3, V3 s1h}, y {V1 s0h, V0 s2, V2 s3, V4 s1h}, z {V2 s0h, V0 s2, V1 s3, V5 s1h}
+    const int vq[3][4] = {{0, 1, 2, 3}, {1, 0, 2, 4}, {2, 0, 1, 5}};
+    const int vs[4] = {0, 2, 3, 1}, vh[4] = {1, 0, 0, 1};
+    for (int ax = 0; ax < 3; ax++)
+        for (int q = 0; q < 4; q++) {
+            t.arr[ax][q] = a.tmpT[tq[ax][q]];
+            t.slot[ax][q] = ax == 2 ? tz_s[q] : ts[q];
+            t.half[ax][q] = th[q];
+            v.arr[ax][q] = a.tmpV[vq[ax][q]];
+            v.slot[ax][q] = vs[q];
+            v.half[ax][q] = vh[q];
+        }
+    k_gather<S, R, 0><<<ggrid, block, 0, st>>>(g, p, a, t, zc, first);
+    k_gather<S, R, 1><<<ggrid, block, 0, st>>>(g, p, a, v, zc, first);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 template <class S>
-cudaError_t adj_step_t(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st) {
     switch (g.R) {
-        case 1: return adj_t_r<S, 1>(g, p, a, st);
-        case 2: return adj_t_r<S, 2>(g, p, a, st);
-        case 3: return adj_t_r<S, 3>(g, p, a, st);
-        case 4: return adj_t_r<S, 4>(g, p, a, st);
-    }
-    return cudaErrorInvalidValue;
-}
-template <class S>
-cudaError_t adj_step_v(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
-    switch (g.R) {
-        case 1: return adj_v_r<S, 1>(g, p, a, st);
-        case 2: return adj_v_r<S, 2>(g, p, a, st);
-        case 3: return adj_v_r<S, 3>(g, p, a, st);
-        case 4: return adj_v_r<S, 4>(g, p, a, st);
+        case 1: return adj_r<S, 1>(g, p, a, first, st);
+        case 2: return adj_r<S, 2>(g, p, a, first, st);
+        case 3: return adj_r<S, 3>(g, p, a, first, st);
+        case 4: return adj_r<S, 4>(g, p, a, first, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -471,9 +527,9 @@ cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, 
     return cudaGetLastError();
 }
 template <class S>
-cudaError_t adj_point(const AdjPtrs& a, long long o, int kind, int phase, double fac, const float* w, int nw, int it,
-                      double* gw, double* gfac, cudaStream_t st) {
-    k_adj_point<typename Traits<S>::C><<<1, 1, 0, st>>>(a, o, kind, phase, fac, w, nw, it, gw, gfac);
+cudaError_t adj_point(const AdjPtrs& a, long long o, int kind, double fac, const float* w, int nw, int it, double* gw,
+                      double* gfac, cudaStream_t st) {
+    k_adj_point<typename Traits<S>::C><<<1, 1, 0, st>>>(a, o, kind, fac, w, nw, it, gw, gfac);
     return cudaGetLastError();
 }
 template <class A>
@@ -486,12 +542,11 @@ cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st) {
 }
 
 #define BEHF_ADJ_INST(S)                                                                                         \
-    template cudaError_t adj_step_t<S>(const Geom&, const DevPtrs&, const AdjPtrs&, cudaStream_t);             \
-    template cudaError_t adj_step_v<S>(const Geom&, const DevPtrs&, const AdjPtrs&, cudaStream_t);             \
+    template cudaError_t adj_step<S>(const Geom&, const DevPtrs&, const AdjPtrs&, int, cudaStream_t);          \
     template cudaError_t adj_record<S>(const AdjPtrs&, const long long*, const int*, int, const double*, int, int, \
                                        const AdjScales&, cudaStream_t);                                          \
-    template cudaError_t adj_point<S>(const AdjPtrs&, long long, int, int, double, const float*, int, int,      \
-                                      double*, double*, cudaStream_t);
+    template cudaError_t adj_point<S>(const AdjPtrs&, long long, int, double, const float*, int, int, double*,  \
+                                      double*, cudaStream_t);
 BEHF_ADJ_INST(double)
 BEHF_ADJ_INST(float)
 BEHF_ADJ_INST(__half)

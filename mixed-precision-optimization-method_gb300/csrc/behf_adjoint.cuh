@@ -4,12 +4,13 @@
 // storage units + CPML memory).  Its adjoint runs  record^T -> T^T -> force^T -> V^T -> source^T  on
 // adjoint fields of the forward arithmetic type A (float, or double for FP64 storage), and accumulates
 // the gradient with respect to each effective coefficient (stored value x power-of-two multiplier) on
-// cells outside every CPML slab.  Each of T^T and V^T is three launches:
-//   1. per cell: adjoints of the derivative groups (7 for T, 6 for V) into tmp[], coefficient gradients
+// cells outside every CPML slab.  The pieces:
+//   per cell: adjoints of the derivative groups (7 for T, 6 for V) into tmpT / tmpV, coefficient gradients
 //      from the forward snapshot of this step;
-//   2. gather: each field's adjoint takes minus the transposed stencils of the derivative adjoints of its
+//   gather: each field's adjoint takes minus the transposed stencils of the derivative adjoints of its
 //      neighbours, each corrected on the fly by the adjoint CPML memory of the neighbour's slab;
-//   3. per slab cell: the adjoint CPML memory update  L = lpsi + lD;  lpsi = A L;  lprev = A B L.
+//   per slab cell: the adjoint CPML memory update  L = lpsi + lD;  lpsi = A L;  lprev = A B L;
+// fused into three launches per step (adjoint.cu).
 #pragma once
 #include "behf_internal.cuh"
 
@@ -19,7 +20,8 @@ struct AdjPtrs {
     void* lf[kNField];       // adjoint fields, type A, pitched like the forward fields
     void* lpsi[3][8];        // adjoint CPML memory, type A, slab layout of the forward memory
     void* lprv[3][8];
-    void* tmp[7];            // per-cell derivative-group adjoints, type A, pitched (zero off the updated cells)
+    void* tmpT[7];           // per-cell derivative-group adjoints of T^T and V^T, type A, pitched
+    void* tmpV[6];           // (zero off the updated cells)
     void* g[kNCoef];         // gradient accumulators per effective coefficient, type A, pitched
     const void* cur[kNField];  // forward snapshot of this step after V (and the force source), type S
     const void* qprev[3];    // q before V of this step, type S
@@ -30,18 +32,18 @@ struct AdjScales {
     double s[kNField];       // multiplier of the adjoint source per recorded field (alpha / storage scale)
 };
 
-// T^T and V^T of one step (three launches each).
-template <class S> cudaError_t adj_step_t(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st);
-template <class S> cudaError_t adj_step_v(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st);
+// T^T and V^T of one step (three launches); first = 1 on the first backward step (no V-slot memory pending).
+template <class S>
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st);
 // record^T: lf[comp[r]][off[r]] += adj[r * nt + it] * sc.s[comp[r]]  (atomic: receivers may share a cell)
 template <class S>
 cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, int nrec, const double* adj, int nt,
                        int it, const AdjScales& sc, cudaStream_t st);
-// source^T at one cell.  phase 0 (after T^T, force source): gw[it] = fac * lvz, gfac += w[it] * lvz (it < nw).
-// phase 1 (after V^T): explosive gw[it] = fac * (lsxx + lsyy + lszz), pressure gw[it] = fac * lp.
+// source^T at one cell after the step: force gw[it] = fac * lvz, gfac += w[it] * lvz (it < nw); explosive
+// gw[it] = fac * (lsxx + lsyy + lszz); pressure gw[it] = fac * lp.
 template <class S>
-cudaError_t adj_point(const AdjPtrs& a, long long o, int kind, int phase, double fac, const float* w, int nw, int it,
-                      double* gw, double* gfac, cudaStream_t st);
+cudaError_t adj_point(const AdjPtrs& a, long long o, int kind, double fac, const float* w, int nw, int it, double* gw,
+                      double* gfac, cudaStream_t st);
 
 // Coefficient-build transpose (main.cpp:322-494 formulas): moduli gradient gm[9][nz][ny][nx] (double,
 // unpitched) from the effective-coefficient gradients g[] (ratio[] = effective / physical coefficient),

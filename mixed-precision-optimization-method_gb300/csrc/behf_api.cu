@@ -988,7 +988,8 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     AdjPtrs a{};
     behf_status st = BEHF_OK;
     for (int q = 0; q < kNField && !st; q++) st = buf.get(&a.lf[q], nf * asz);
-    for (int q = 0; q < 7 && !st; q++) st = buf.get(&a.tmp[q], nf * asz);
+    for (int q = 0; q < 7 && !st; q++) st = buf.get(&a.tmpT[q], nf * asz);
+    for (int q = 0; q < 6 && !st; q++) st = buf.get(&a.tmpV[q], nf * asz);
     for (int q = 0; q < kNCoef && !st; q++) st = buf.get(&a.g[q], nf * asz);
     if (g.W > 0)
         for (int ax = 0; ax < 3 && !st; ax++)
@@ -1011,7 +1012,8 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     if (!st) st = buf.get((void**)&d_gfac, 8);
     if (st) return st;
     for (int q = 0; q < kNField; q++) CK(cudaMemsetAsync(a.lf[q], 0, nf * asz, c->stream));
-    for (int q = 0; q < 7; q++) CK(cudaMemsetAsync(a.tmp[q], 0, nf * asz, c->stream));
+    for (int q = 0; q < 7; q++) CK(cudaMemsetAsync(a.tmpT[q], 0, nf * asz, c->stream));
+    for (int q = 0; q < 6; q++) CK(cudaMemsetAsync(a.tmpV[q], 0, nf * asz, c->stream));
     for (int q = 0; q < kNCoef; q++) CK(cudaMemsetAsync(a.g[q], 0, nf * asz, c->stream));
     if (g.W > 0)
         for (int ax = 0; ax < 3; ax++)
@@ -1113,11 +1115,9 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(it - s0 + 1, f);
             for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(it - s0, BEHF_QX + d);
             CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
-            CK(adj_step_t<S>(g, c->p, a, c->stream));
-            CK(adj_point<S>(a, so, c->src_kind, 0, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
-            CK(adj_step_v<S>(g, c->p, a, c->stream));
-            CK(adj_point<S>(a, so, c->src_kind, 1, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
-            c->launches += g.W > 0 ? 9 : 7;
+            CK(adj_step<S>(g, c->p, a, it == nt - 1 ? 1 : 0, c->stream));
+            CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
+            c->launches += 5;
         }
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));

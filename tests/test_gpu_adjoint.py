@@ -136,3 +136,24 @@ def test_gradient_errors(behf_lib):
     with pytest.raises(behf.BehfError):
         s.gradient(p.nt, np.zeros((len(p.rec_comp), p.nt)))
     s.close()
+
+
+def test_torch_autograd_wrapper(behf_lib):
+    torch = pytest.importorskip("torch")
+    from behf import torch_ops
+    p = small(R=2, L=4, kind="explosive")
+    rng = np.random.default_rng(8)
+    dobs = rng.standard_normal((len(p.rec_comp), p.nt)) * 1e-3
+    sim = torch_ops.Simulation(p, precision="f64")
+    mod = torch.tensor(p.mod, device="cuda", requires_grad=True)
+    w = torch.tensor(p.wavelet, requires_grad=True)
+    seis = sim(mod, w)
+    loss = 0.5 * ((seis - torch.from_numpy(dobs)) ** 2).sum()
+    loss.backward()
+    sim.close()
+    s = behf.solver_for(p, precision="f64", gradient=True)
+    J, gw, gm = s.misfit_gradient(p.nt, dobs)
+    s.close()
+    assert abs(loss.item() - J) <= 1e-10 * J
+    assert rel(mod.grad.double().cpu().numpy(), gm.astype(np.float32).astype(np.float64)) < 1e-6
+    assert rel(w.grad.double().numpy(), gw.astype(np.float32).astype(np.float64)) < 1e-6
