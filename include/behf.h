@@ -91,6 +91,7 @@ enum {
     BEHF_OPT_GRADIENT = 3,       /* 1: keep the cell-centred moduli on the device (9 x 4 B per cell) so that
                                     behf_gradient can map coefficient gradients to moduli; set before the medium */
     BEHF_OPT_CHECKPOINT = 4,     /* steps between checkpoints of the gradient's forward pass (0 = round(sqrt(nt))) */
+    BEHF_OPT_ZCHUNK = 5,         /* tiled kernels: z planes each CTA marches (0 = enough chunks to fill every SM) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current
@@ -213,6 +214,16 @@ behf_status behf_gradient(behf_ctx* ctx, int nt, const double* adj_src, double* 
  * adjoint source is the residual of the forward pass; J is written to *misfit. */
 behf_status behf_misfit_gradient(behf_ctx* ctx, int nt, const double* observed, double* misfit,
                                  double* grad_wavelet, double* const grad_moduli[BEHF_NMOD]);
+
+/* Autotuner (no counterpart in the reference): times trial_steps steps for each z-chunk length of the tiled
+ * kernels (BEHF_OPT_ZCHUNK candidates 0, 16, 32, ... up to the grid), keeps the fastest, and resets the
+ * wavefields (behf_reset).  Writes the chosen value and its milliseconds per step. */
+behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, double* ms_per_step_out);
+
+/* Batched shots on one GPU (no counterpart in the reference): advances n independent contexts by nsteps each,
+ * enqueuing graph-chunk-sized pieces round-robin on their own streams so the shots overlap on the device, then
+ * waits for all.  Equivalent to behf_run on each context in turn. */
+behf_status behf_run_batch(behf_ctx* const* ctxs, int n, int nsteps);
 
 /* Text of the last error on this thread. */
 const char* behf_last_error(void);

@@ -22,7 +22,7 @@ MODULI = ["rho", "rhof", "mu", "M", "C", "HH", "H2u", "C1", "C2"]
 PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
-OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT = 0, 1, 2, 3, 4
+OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK = 0, 1, 2, 3, 4, 5
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -116,6 +116,8 @@ def load() -> C.CDLL:
         "behf_gradient": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double), P(P(C.c_double))],
         "behf_misfit_gradient": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double),
                                  P(P(C.c_double))],
+        "behf_autotune": [C.c_void_p, C.c_int, P(C.c_int), P(C.c_double)],
+        "behf_run_batch": [P(C.c_void_p), C.c_int, C.c_int],
         "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                     C.c_void_p, C.c_void_p, C.c_void_p],
     }
@@ -275,6 +277,12 @@ class Solver:
         _check(self._lib.behf_time_kernels(self._ctx, int(nsteps), ms.ctypes.data_as(C.POINTER(C.c_double))))
         return {"source": ms[0], "velocity": ms[1], "stress": ms[2], "record": ms[3]}
 
+    def autotune(self, trial_steps: int = 4):
+        """Pick the fastest z-chunk length of the tiled kernels; resets the wavefields.  Returns (zchunk, ms/step)."""
+        z, ms = C.c_int(0), C.c_double(0)
+        _check(self._lib.behf_autotune(self._ctx, int(trial_steps), C.byref(z), C.byref(ms)))
+        return z.value, ms.value
+
     # -- gradient (adjoint state, checkpointed)
     def enable_gradient(self, checkpoint: int = 0):
         """Keep the moduli on the device for behf_gradient (call before the medium); checkpoint = steps
@@ -348,6 +356,12 @@ def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:
     return {"velocity": vel, "stress": strs, "step_unfused": vel + strs, "step_fused": fused}
 
 
+def run_batch(solvers, nsteps: int):
+    """Advance independent solvers (shots) together on the device: their streams overlap."""
+    arr = (C.c_void_p * len(solvers))(*[s._ctx.value for s in solvers])
+    _check(load().behf_run_batch(arr, len(solvers), int(nsteps)))
+
+
 def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None, gradient=False,
                checkpoint=0) -> Solver:
     """A Solver set up with a problem description (see behf.problems.Problem); gradient=True keeps what
@@ -371,4 +385,4 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
     return s
 
 
-__all__ = ["Solver", "BehfError", "solver_for", "load", "lib_path", "FIELDS", "FIELD", "MODULI"]
+__all__ = ["Solver", "BehfError", "solver_for", "run_batch", "load", "lib_path", "FIELDS", "FIELD", "MODULI"]

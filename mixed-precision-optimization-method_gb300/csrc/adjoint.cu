@@ -148,11 +148,12 @@ struct G25 {
     typedef typename Traits<S>::C A;
     static constexpr int XW = GX + 2 * R;
     static constexpr int YH = GY + 2 * R;
+    template <bool CHK>
     static __device__ __forceinline__ A corr(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const void* arr,
                                              int ax, int slot, int half, int x, int y, int k) {
         if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) return (A)0;
         A v = reinterpret_cast<const A*>(arr)[(long long)k * g.plane + (long long)y * g.px + x];
-        if (g.W > 0) {
+        if (CHK && g.W > 0) {
             const int pos = ax == 0 ? x : ax == 1 ? y : k;
             const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
             if (s >= 0) {
@@ -163,6 +164,18 @@ struct G25 {
             }
         }
         return v;
+    }
+    // the CPML correction of a value already loaded (two independent loads on slab cells)
+    static __device__ __forceinline__ A fix(const Geom& g, const DevPtrs& p, const AdjPtrs& a, A v, int ax, int slot,
+                                            int half, int x, int y, int k) {
+        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) return v;
+        const int pos = ax == 0 ? x : ax == 1 ? y : k;
+        const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
+        if (s < 0) return v;
+        const long long so = slab_off(g, ax, x, y, k, s);
+        const A B = reinterpret_cast<const A*>(half ? p.pb2[ax] : p.pb[ax])[pos];
+        return v + B * (reinterpret_cast<const A*>(a.lpsi[ax][slot])[so] + v) +
+               reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
     }
     // w[d + R] = L[c + d]:  fwdL = sum_m w_m (L[+m] - L[1-m]),  bwdL = sum_m w_m (L[m-1] - L[-m])
     template <class F>
@@ -186,7 +199,7 @@ struct G25 {
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
 //                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update.
 template <class S, int R, int KIND>
-__global__ void __launch_bounds__(256) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc, int first) {
+__global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc, int first) {
     typedef G25<S, R> W;
     typedef Adj<S, R> Q;
     typedef typename W::A A;
@@ -204,22 +217,61 @@ __global__ void __launch_bounds__(256) k_gather(Geom g, DevPtrs p, AdjPtrs a, St
         for (int q = 0; q < 4; q++)
 #pragma unroll
             for (int d = 0; d < 2 * R; d++)
-                zq[q][d] = W::corr(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, kb - R + d);
+                zq[q][d] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
+                                                  kb - R + d);
     }
     const long long sy = g.px, sz = g.plane;
+    constexpr int NXE = 4 * GY * W::XW, NYE = 4 * W::YH * GX, NT = GX * GY;
+    constexpr int IX = (NXE + NT - 1) / NT, IY = (NYE + NT - 1) / NT;
+    // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
+    const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
+    const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
     for (int k = kb; k < ke; k++) {
-        for (int e = t; e < 4 * GY * W::XW; e += GX * GY) {
-            const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
-            shx[q][r][cc] = W::corr(g, p, a, ss.arr[0][q], 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
+        {  // every load of the plane in flight together, then (near a slab) the corrections, then the stores
+            A v[IX];
+#pragma unroll
+            for (int u = 0; u < IX; u++) {
+                const int e = t + u * NT;
+                const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
+                if (e < NXE) v[u] = W::template corr<false>(g, p, a, ss.arr[0][q], 0, 0, 0, i0 - R + cc, j0 + r, k);
+            }
+            if (cx) {
+#pragma unroll
+                for (int u = 0; u < IX; u++) {
+                    const int e = t + u * NT;
+                    const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
+                    if (e < NXE) v[u] = W::fix(g, p, a, v[u], 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < IX; u++)
+                if (t + u * NT < NXE) (&shx[0][0][0])[t + u * NT] = v[u];
         }
-        for (int e = t; e < 4 * W::YH * GX; e += GX * GY) {
-            const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
-            shy[q][r][cc] = W::corr(g, p, a, ss.arr[1][q], 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
+        {
+            A v[IY];
+#pragma unroll
+            for (int u = 0; u < IY; u++) {
+                const int e = t + u * NT;
+                const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
+                if (e < NYE) v[u] = W::template corr<false>(g, p, a, ss.arr[1][q], 1, 0, 0, i0 + cc, j0 - R + r, k);
+            }
+            if (cy) {
+#pragma unroll
+                for (int u = 0; u < IY; u++) {
+                    const int e = t + u * NT;
+                    const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
+                    if (e < NYE) v[u] = W::fix(g, p, a, v[u], 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < IY; u++)
+                if (t + u * NT < NYE) (&shy[0][0][0])[t + u * NT] = v[u];
         }
         if (valid) {
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                zq[q][2 * R] = W::corr(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, k + R);
+                zq[q][2 * R] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
+                                                      k + R);
         }
         __syncthreads();
         if (valid) {
@@ -472,7 +524,7 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
     const dim3 grid((nxu + 31) / 32, (nyu + 7) / 8, nzu);
     k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a);
-    // gathers: z chunks so that about four CTAs per SM are resident
+    // gathers: z chunks so that about eight CTAs per SM are launched
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -481,7 +533,7 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
         if (sms <= 0) sms = 132;
     }
     const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
-    int nch = (4 * sms + nxy - 1) / nxy;
+    int nch = (8 * sms + nxy - 1) / nxy;
     nch = std::max(1, std::min(nch, std::max(1, nzu / 8)));
     const int zc = (nzu + nch - 1) / nch;
     const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);

@@ -1,6 +1,7 @@
 // behf_api.cu -- the C ABI of libbehf (include/behf.h): context, device memory, set-up and the
 // graph-captured time loop.  Replaces the reference's host/device boundary: main.cpp:1529-1743
 // (allocation and copies of the blockInfo arrays) and callCUDAKernel (kernel.cu:1728-2698).
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstdarg>
@@ -491,6 +492,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.px = ((long long)gr->nx + 15) / 16 * 16;
     g.plane = g.px * gr->ny;
     g.bug = 0;
+    g.zchunk_req = 0;
     c->nfield = g.plane * gr->nz;
     bool all0 = true;
     for (int s = 0; s < 4; s++) all0 = all0 && gr->scales[s] == 0;
@@ -829,6 +831,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
         case BEHF_OPT_CHECKPOINT:
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative checkpoint spacing");
             c->ck_stride = value;
+            break;
+        case BEHF_OPT_ZCHUNK:
+            if (value < 0) return fail(BEHF_ERR_INVALID, "negative z chunk");
+            c->g.zchunk_req = value;
             break;
         default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
     }
@@ -1223,6 +1229,76 @@ behf_status behf_misfit_gradient(behf_ctx* c, int nt, const double* observed, do
                                  double* const grad_moduli[BEHF_NMOD]) {
     if (!c || !observed) return fail(BEHF_ERR_INVALID, "null argument");
     return gradient_dispatch(c, nt, nullptr, observed, misfit, grad_wavelet, grad_moduli);
+}
+
+behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double* ms_out) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_autotune");
+    if (trial_steps < 1) return fail(BEHF_ERR_INVALID, "trial_steps must be positive");
+    const int planes = c->grid.nz - 2 * c->g.R;
+    std::vector<int> cand = {0};
+    for (int z = 16; z < planes; z *= 2) cand.push_back(z);
+    cand.push_back(planes);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double best = 1e300;
+    int best_z = 0;
+    behf_status st = BEHF_OK;
+    const int nrec = c->nrec;
+    c->nrec = 0;  // trial steps record nothing
+    for (int z : cand) {
+        c->g.zchunk_req = z;
+        c->invalidate_graph();
+        if ((st = zero_state(c))) break;
+        if ((st = behf_run_async(c, 1))) break;
+        cudaEventRecord(e0, c->stream);
+        if ((st = behf_run_async(c, trial_steps))) break;
+        cudaEventRecord(e1, c->stream);
+        if ((st = behf_sync(c))) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms / trial_steps < best) {
+            best = ms / trial_steps;
+            best_z = z;
+        }
+    }
+    c->nrec = nrec;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->g.zchunk_req = best_z;
+    c->invalidate_graph();
+    if (st) return st;
+    st = zero_state(c);
+    if (st) return st;
+    if (zchunk_out) *zchunk_out = best_z;
+    if (ms_out) *ms_out = best;
+    return BEHF_OK;
+}
+
+behf_status behf_run_batch(behf_ctx* const* ctxs, int n, int nsteps) {
+    if (!ctxs || n < 0 || nsteps < 0) return fail(BEHF_ERR_INVALID, "bad batch arguments");
+    for (int i = 0; i < n; i++)
+        if (!ctxs[i]) return fail(BEHF_ERR_INVALID, "context %d is null", i);
+    // round-robin pieces of one graph chunk per context so the contexts' streams overlap on the device
+    int done = 0;
+    while (done < nsteps) {
+        int piece = nsteps - done;
+        for (int i = 0; i < n; i++) {
+            const int ch = ctxs[i]->chunk > 0 ? ctxs[i]->chunk : 16;
+            piece = std::min(piece, ch);
+        }
+        for (int i = 0; i < n; i++) {
+            behf_status st = behf_run_async(ctxs[i], piece);
+            if (st) return st;
+        }
+        done += piece;
+    }
+    for (int i = 0; i < n; i++) {
+        behf_status st = behf_sync(ctxs[i]);
+        if (st) return st;
+    }
+    return BEHF_OK;
 }
 
 }  // extern "C"

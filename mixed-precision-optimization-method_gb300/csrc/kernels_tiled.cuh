@@ -22,8 +22,11 @@
 namespace behf {
 namespace tiled {
 
+#ifndef BEHF_TILED_TY
+#define BEHF_TILED_TY 8
+#endif
 constexpr int TXC = 64;            // cells per tile row (x)
-constexpr int TY = 8;              // tile rows (y)
+constexpr int TY = BEHF_TILED_TY;  // tile rows (y), one warp each
 constexpr int NTH = 32 * TY;       // threads per CTA
 constexpr long long kSpinLimit = 4000000000LL;  // clock64 cycles (~2 s) before a wait gives up
 

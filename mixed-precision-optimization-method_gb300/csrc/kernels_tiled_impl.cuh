@@ -620,7 +620,8 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     nzc = nzc < 1 ? 1 : nzc;
     const int maxc = planes / 16 > 1 ? planes / 16 : 1;
     nzc = nzc > maxc ? maxc : nzc;
-    const int zchunk = (planes + nzc - 1) / nzc;
+    int zchunk = (planes + nzc - 1) / nzc;
+    if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
         const int smem = Map<S, R, true>::bytes + 128;
