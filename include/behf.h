@@ -91,7 +91,11 @@ enum {
     BEHF_OPT_GRADIENT = 3,       /* 1: keep the cell-centred moduli on the device (9 x 4 B per cell) so that
                                     behf_gradient can map coefficient gradients to moduli; set before the medium */
     BEHF_OPT_CHECKPOINT = 4,     /* steps between checkpoints of the gradient's forward pass (0 = round(sqrt(nt))) */
-    BEHF_OPT_ZCHUNK = 5,         /* tiled kernels: z planes each CTA marches (0 = enough chunks to fill every SM) */
+    BEHF_OPT_ZCHUNK = 5,         /* tiled kernels: z planes each CTA marches (0 = automatic: at most 64, fewer when
+                                    needed to give every SM work) */
+    BEHF_OPT_COEF_ROUNDING = 6,  /* FP16/BF16 kinds, set before the medium: 0 coefficients rounded to nearest,
+                                    1 unbiased (hash-dithered) rounding that removes the wave-speed bias of
+                                    coherent rounding in homogeneous regions */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current

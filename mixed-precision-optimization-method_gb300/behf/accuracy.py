@@ -22,8 +22,8 @@ from . import FIELDS, solver_for
 from . import problems
 
 
-def run_one(prob, precision: str, kernel: str = "auto"):
-    s = solver_for(prob, precision, kernel)
+def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0):
+    s = solver_for(prob, precision, kernel, coef_rounding=coef_rounding if precision in ("f16", "bf16") else 0)
     t0 = time.perf_counter()
     s.run(prob.nt)
     wall = time.perf_counter() - t0
@@ -45,6 +45,7 @@ def main(argv=None):
     ap.add_argument("--workload", default="layered256", choices=["layered256", "random1024", "small64"])
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--n", type=int, default=0, help="grid override (test-sized runs)")
+    ap.add_argument("--coef-rounding", type=int, default=0, help="1: unbiased coefficient rounding (16-bit kinds)")
     args = ap.parse_args(argv)
     if args.workload == "layered256":
         prob = problems.layered256(n=args.n or 256, nt=args.steps or 2000)
@@ -55,13 +56,14 @@ def main(argv=None):
     else:
         prob = problems.random1024(n=args.n or 1024, nt=args.steps or 1200, medium=False, nrec_side=128)
         ref_prec, others = "f32", ["f16", "bf16"]
-    out = {"workload": prob.name, "cells": prob.cells, "steps": prob.nt, "reference": ref_prec, "runs": {}}
+    out = {"workload": prob.name, "cells": prob.cells, "steps": prob.nt, "reference": ref_prec, "runs": {},
+           "coef_rounding": args.coef_rounding}
     ref, meta = run_one(prob, ref_prec)
     out["runs"][ref_prec] = meta
     comps = np.unique(prob.rec_comp)
     out["peak"] = {FIELDS[c]: float(np.abs(ref[prob.rec_comp == c]).max()) for c in comps}
     for prec in others:
-        seis, meta = run_one(prob, prec)
+        seis, meta = run_one(prob, prec, coef_rounding=args.coef_rounding)
         meta["rel_l2"] = {FIELDS[c]: rel_l2(seis[prob.rec_comp == c], ref[prob.rec_comp == c]) for c in comps}
         out["runs"][prec] = meta
     print(json.dumps(out))

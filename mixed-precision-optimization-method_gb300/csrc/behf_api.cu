@@ -128,6 +128,7 @@ struct behf_ctx {
     bool keep_medium = false;
     float* d_mod[kNMod] = {};
     int ck_stride = 0;
+    int coef_dither = 0;  // BEHF_OPT_COEF_ROUNDING
 
     ~behf_ctx() {
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -345,6 +346,7 @@ behf_status build_coefs(behf_ctx* c, const float* const mod[kNMod]) {
     a.px = c->g.px;
     a.plane = c->g.plane;
     a.dt = c->grid.dt;
+    a.dither = c->coef_dither;
     const double sv = c->scales[0], sq = c->scales[1], ss = c->scales[2], sp = c->scales[3];
     const double hi = 1.0 / c->grid.h;
     for (int d = 0; d < 3; d++) {
@@ -831,6 +833,11 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
         case BEHF_OPT_CHECKPOINT:
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative checkpoint spacing");
             c->ck_stride = value;
+            break;
+        case BEHF_OPT_COEF_ROUNDING:
+            if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "coefficient rounding must be 0 or 1");
+            if (c->medium_set) return fail(BEHF_ERR_STATE, "BEHF_OPT_COEF_ROUNDING must be set before the medium");
+            c->coef_dither = value;
             break;
         case BEHF_OPT_ZCHUNK:
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative z chunk");

@@ -14,6 +14,7 @@ struct CoefArgs {
     void* out[kNCoef];
     unsigned long long* maxbits;  // pass 0: per-array max |ratio * coef| as double bits
     int pass;
+    int dither;                // 16-bit coefficients: 0 round to nearest, 1 unbiased hash-dithered rounding
 };
 
 struct RecScales {

@@ -99,7 +99,7 @@ struct Geom {
     long long px, plane;   // row pitch and plane stride in elements
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out
-    int zchunk_req;        // tiled kernels: z planes per CTA (0 = enough chunks to fill every SM)
+    int zchunk_req;        // tiled kernels: z planes per CTA (0 = automatic)
     float kmulf[kNCoef];   // power-of-two multipliers of the stored coefficients
     double kmuld[kNCoef];
     // Exact identities the tiled kernels use instead of reading two more arrays (effective, scaled values):

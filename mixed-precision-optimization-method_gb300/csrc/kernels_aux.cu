@@ -76,6 +76,29 @@ __device__ void cell_coefs(const CoefArgs& a, int i, int j, int k, double out[kN
     out[SYZC] = muyz * dt;
 }
 
+// Unbiased rounding of a coefficient to FP16: the two FP16 neighbours a <= s <= b are chosen with
+// probabilities (b - s)/(b - a) and (s - a)/(b - a), decided by a hash of (cell, array), so the rounding errors
+// of a homogeneous region average to zero over a wavelength instead of biasing the wave speed.
+__device__ __half dither_half(double s, long long cell, int q) {
+    const __half a = __float2half_rn((float)s);
+    const double da = (double)__half2float(a);
+    if (da == s) return a;
+    unsigned short ab = __half_as_ushort(a), bb;
+    if ((ab & 0x7fffu) == 0) bb = s > 0 ? 0x0001 : 0x8001;
+    else bb = ((da < s) == !(ab & 0x8000u)) ? (unsigned short)(ab + 1) : (unsigned short)(ab - 1);
+    const __half b = __ushort_as_half(bb);
+    const double db = (double)__half2float(b);
+    const double pb = (s - da) / (db - da);  // in (0, 1/2]
+    unsigned long long h = (unsigned long long)cell * 0x9E3779B97F4A7C15ull + (unsigned long long)(q + 1) * 0xD1B54A32D192ED03ull;
+    h ^= h >> 30;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 27;
+    h *= 0x94D049BB133111EBull;
+    h ^= h >> 31;
+    const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    return u < pb ? b : a;
+}
+
 template <class K, class W>
 __global__ void k_coef(CoefArgs a, int pass) {
     double mx[kNCoef];
@@ -98,7 +121,8 @@ __global__ void k_coef(CoefArgs a, int pass) {
 #pragma unroll
             for (int q = 3; q < kNCoef; q++) {
                 const double s = v[q] * a.ratio[q] * a.inv[q];
-                if constexpr (sizeof(K) == 2) reinterpret_cast<K*>(a.out[q])[o] = __float2half_rn((float)s);
+                if constexpr (sizeof(K) == 2)
+                    reinterpret_cast<K*>(a.out[q])[o] = a.dither ? dither_half(s, c, q) : __float2half_rn((float)s);
                 else reinterpret_cast<K*>(a.out[q])[o] = (K)s;
             }
         }
