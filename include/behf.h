@@ -96,6 +96,9 @@ enum {
     BEHF_OPT_COEF_ROUNDING = 6,  /* FP16/BF16 kinds, set before the medium: 0 coefficients rounded to nearest,
                                     1 unbiased (hash-dithered) rounding that removes the wave-speed bias of
                                     coherent rounding in homogeneous regions */
+    BEHF_OPT_STATE_ROUNDING = 7, /* FP16/BF16 kinds, tiled kernels: 0 fields stored rounded to nearest, 1 stochastic
+                                    rounding (seeded by step, field and cell), which keeps increments smaller than
+                                    half a unit in the last place in expectation instead of dropping them */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current

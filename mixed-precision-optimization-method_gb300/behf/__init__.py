@@ -22,7 +22,8 @@ MODULI = ["rho", "rhof", "mu", "M", "C", "HH", "H2u", "C1", "C2"]
 PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
-OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING = range(7)
+(OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
+ OPT_STATE_ROUNDING) = range(8)
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -363,7 +364,7 @@ def run_batch(solvers, nsteps: int):
 
 
 def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None, gradient=False,
-               checkpoint=0, coef_rounding=0) -> Solver:
+               checkpoint=0, coef_rounding=0, state_rounding=0) -> Solver:
     """A Solver set up with a problem description (see behf.problems.Problem); gradient=True keeps what
     Solver.gradient needs."""
     s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
@@ -377,6 +378,8 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
         s.enable_gradient(checkpoint)
     if coef_rounding:
         s.set_option(OPT_COEF_ROUNDING, int(coef_rounding))
+    if state_rounding:
+        s.set_option(OPT_STATE_ROUNDING, int(state_rounding))
     if prob.mod.shape[1:] == (prob.nz, prob.ny, prob.nx):
         s.set_medium(prob.mod)
     else:

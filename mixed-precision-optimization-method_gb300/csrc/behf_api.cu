@@ -248,6 +248,7 @@ cudaError_t enqueue_steps_t(behf_ctx* c, int n, double fac) {
             e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, s, fac, c->stream);
             if (e != cudaSuccess) return e;
         }
+        c->g.step_off = s;
         {
             TimedLaunch t(c, 1);
             if ((e = dispatch_update(c, true)) != cudaSuccess) return e;
@@ -261,6 +262,7 @@ cudaError_t enqueue_steps_t(behf_ctx* c, int n, double fac) {
             TimedLaunch t(c, 2);
             if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
         }
+        c->g.step_off = 0;
         if (c->nrec > 0) {
             TimedLaunch t(c, 3);
             if ((e = aux_record<S>(c->p, c->d_rec_off, c->d_rec_comp, c->nrec, c->d_seis, c->cap, c->d_it, s, rs,
@@ -495,6 +497,9 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.plane = g.px * gr->ny;
     g.bug = 0;
     g.zchunk_req = 0;
+    g.sr = 0;
+    g.step = nullptr;
+    g.step_off = 0;
     c->nfield = g.plane * gr->nz;
     bool all0 = true;
     for (int s = 0; s < 4; s++) all0 = all0 && gr->scales[s] == 0;
@@ -552,6 +557,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     }
     if (st == BEHF_OK && cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) st = BEHF_ERR_CUDA;
     g.err = c->d_err;
+    g.step = c->d_it;
     if (st == BEHF_OK) st = upload_profiles(c);
     if (st == BEHF_OK) st = zero_state(c);
     if (st == BEHF_OK) {
@@ -838,6 +844,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "coefficient rounding must be 0 or 1");
             if (c->medium_set) return fail(BEHF_ERR_STATE, "BEHF_OPT_COEF_ROUNDING must be set before the medium");
             c->coef_dither = value;
+            break;
+        case BEHF_OPT_STATE_ROUNDING:
+            if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "state rounding must be 0 or 1");
+            c->g.sr = (c->prec == BEHF_FP16 || c->prec == BEHF_BF16) ? value : 0;
             break;
         case BEHF_OPT_ZCHUNK:
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative z chunk");

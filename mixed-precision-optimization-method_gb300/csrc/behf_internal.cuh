@@ -100,6 +100,9 @@ struct Geom {
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out
     int zchunk_req;        // tiled kernels: z planes per CTA (0 = automatic)
+    int sr;                // 16-bit kinds, tiled kernels: stochastic rounding of the stored fields
+    const int* step;       // device step counter (seeds the stochastic rounding)
+    int step_off;          // step offset of this launch within a graph chunk
     float kmulf[kNCoef];   // power-of-two multipliers of the stored coefficients
     double kmuld[kNCoef];
     // Exact identities the tiled kernels use instead of reading two more arrays (effective, scaled values):

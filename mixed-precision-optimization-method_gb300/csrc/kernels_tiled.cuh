@@ -50,6 +50,43 @@ template <> struct Pair<float> {
     static __device__ __forceinline__ float one(float v) { return v; }
 };
 
+// Stochastic rounding of a float pair to the 16-bit storage types, from 32 random bits r (16 per value for
+// BF16, 13 per value for FP16): a value between two representable neighbours goes to the upper one with
+// probability equal to its distance from the lower one, so rounding errors average out over the steps instead
+// of dropping increments smaller than half a unit in the last place.  Adding the random bits below the kept
+// mantissa bits and truncating does exactly that for normal numbers; FP16 subnormals (|x| < 2^-14) and
+// non-finite values are rounded to nearest.
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float sr_trunc(float x, uint32_t r, int drop) {
+    const uint32_t u = __float_as_uint(x), mask = (1u << drop) - 1u;
+    return __uint_as_float((u + (r & mask)) & ~mask);
+}
+template <class S> struct SR;
+template <> struct SR<__half> {
+    static __device__ __forceinline__ __half2 pack(float2 v, uint32_t r) {
+        const float a = fabsf(v.x) >= 6.103515625e-05f && fabsf(v.x) < 65504.f ? sr_trunc(v.x, r, 13) : v.x;
+        const float b = fabsf(v.y) >= 6.103515625e-05f && fabsf(v.y) < 65504.f ? sr_trunc(v.y, r >> 16, 13) : v.y;
+        return __floats2half2_rn(a, b);
+    }
+};
+template <> struct SR<__nv_bfloat16> {
+    static __device__ __forceinline__ __nv_bfloat162 pack(float2 v, uint32_t r) {
+        const float a = isfinite(v.x) ? sr_trunc(v.x, r, 16) : v.x;
+        const float b = isfinite(v.y) ? sr_trunc(v.y, r >> 16, 16) : v.y;
+        return __floats2bfloat162_rn(a, b);
+    }
+};
+template <> struct SR<float> {
+    static __device__ __forceinline__ float2 pack(float2 v, uint32_t) { return v; }
+};
+
 // Box geometry in elements.  X boxes carry an x halo of HX = 16 bytes each side, Y boxes a y halo of R
 // rows, XY boxes both; own-cell boxes are TXC x TY.
 template <class S, int R>

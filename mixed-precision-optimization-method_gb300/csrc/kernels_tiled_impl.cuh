@@ -240,6 +240,8 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
     const int oe = ty * TXC + xl;  // element offset of the pair in an own-cell box
+    // stochastic-rounding seed of this step (velocity and stress draw different bits)
+    const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x2545f491u) : 0u;
 
     if (tid == 0) {
         for (int s = 0; s < NS; s++) {
@@ -278,6 +280,23 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it % NS;
+        // the cell's own data of plane k (v, q, VW1 in FP32, VW3, VU1, VU2) does not go through the pipeline:
+        // its loads are issued before the waits so that their latency overlaps them and the stencils
+        const long long go = (long long)k * g.plane + col;
+        P vo_s[3], qo_s[3];
+        float2 vw1[3];
+        KP kw3[3], ku1[3], ku2[3];
+        if (live) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
+                qo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_QX + a]) + go);
+                vw1[a] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.k[VW1X + a]) + go);
+                kw3[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VW3X + a]) + go);
+                ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
+                ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
+            }
+        }
         bool ok = true;
         if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
         if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
@@ -289,21 +308,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         if (tid == 0) pp.pend[st]--;
         const unsigned char* b = smem + st * M::stage;
         if (live) {
-            const long long go = (long long)k * g.plane + col;
-            // private data first: v, q, VW1 (FP32), VW3, VU1, VU2 -- consumed after the stencils
-            P vo_s[3], qo_s[3];
-            float2 vw1[3];
-            KP kw3[3], ku1[3], ku2[3], kw3y;
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
-                qo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_QX + a]) + go);
-                vw1[a] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.k[VW1X + a]) + go);
-                kw3[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VW3X + a]) + go);
-                ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
-                ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
-            }
-            kw3y = kw3[1];
             const S* txx = reinterpret_cast<const S*>(b + M::halo(0));
             const S* tyy = reinterpret_cast<const S*>(b + M::halo(1));
             const S* txy = reinterpret_cast<const S*>(b + M::halo(2));
@@ -361,17 +365,20 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
                 const float2 vw3 = km(kw3[a], VW3X + a);
                 const float2 vu1 = km(ku1[a], VU1X + a), vu2 = km(ku2[a], VU2X + a);
                 const float2 vw2 = mul2(mul2(vu2, vw3), f2(g.c_vw2, g.c_vw2));
-                const float2 vw3p = (a == 2 && g.bug) ? km(kw3y, VW3Y) : vw3;  // reference: vz uses VW3y
+                const float2 vw3p = (a == 2 && g.bug) ? km(kw3[1], VW3Y) : vw3;  // reference: vz uses VW3y
                 const float2 qo = PS::f2(qo_s[a]);
                 // q' = VW1 q - VW2 sum(d sigma) - VW3 d p
                 const float2 t = fma2(vw2, sum[a], mul2(vw3p, dp[a]));
                 const float2 qn = fma2(vw1[a], qo, make_float2(-t.x, -t.y));
-                const P qs = PS::pack(qn);
+                const P qs = g.sr ? SR<S>::pack(qn, mix32(seed ^ (uint32_t)go ^ (0x3c6ef372u * (uint32_t)(a + 1))))
+                                  : PS::pack(qn);
                 store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_QX + a]) + go, qs, a0, a1);
                 // v' = v + VU1 sum(d sigma) - VU2 (q' - q)
                 const float2 dq = sub2(PS::f2(qs), qo);
                 const float2 vn = fma2(vu1, sum[a], fma2(make_float2(-vu2.x, -vu2.y), dq, PS::f2(vo_s[a])));
-                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, PS::pack(vn), a0, a1);
+                const P vs = g.sr ? SR<S>::pack(vn, mix32(seed ^ (uint32_t)go ^ (0x1b873593u * (uint32_t)(a + 1))))
+                                  : PS::pack(vn);
+                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, vs, a0, a1);
             }
         }
         __syncwarp();
@@ -406,6 +413,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
     const int oe = ty * TXC + xl;
+    const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x6a09e667u) : 0u;
 
     if (tid == 0) {
         for (int s = 0; s < NS; s++) {
@@ -443,6 +451,19 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it % NS;
+        // the cell's own data of plane k (seven stresses/pressure, P1 P2 S1 S2 Sxy Sxz Syz; S3 = P1 c_s3) does not
+        // go through the pipeline: its loads are issued before the waits
+        const long long go = (long long)k * g.plane + col;
+        P so_s[7];
+        KP kk[7];
+        if (live) {
+#pragma unroll
+            for (int q = 0; q < 7; q++) {
+                so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
+                const int j = q < 4 ? P1 + q : P1 + q + 1;
+                kk[q] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[j]) + go);
+            }
+        }
         bool ok = true;
         if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
         if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
@@ -454,16 +475,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         if (tid == 0) pp.pend[st]--;
         const unsigned char* b = smem + st * M::stage;
         if (live) {
-            const long long go = (long long)k * g.plane + col;
-            // private data first: the seven stresses/pressure and P1 P2 S1 S2 Sxy Sxz Syz
-            P so_s[7];
-            KP kk[7];
-#pragma unroll
-            for (int q = 0; q < 7; q++) {
-                so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
-                const int j = q < 4 ? P1 + q : P1 + q + 1;  // skip S3 (= P1 c_s3)
-                kk[q] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[j]) + go);
-            }
             const S* vx = reinterpret_cast<const S*>(b + M::halo(0));
             const S* vy = reinterpret_cast<const S*>(b + M::halo(1));
             const S* vz = reinterpret_cast<const S*>(b + M::halo(2));
@@ -519,7 +530,9 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             };
             auto own = [&](int q) { return PS::f2(so_s[q]); };
             auto put = [&](int field, float2 v) {
-                store_pair<S>(reinterpret_cast<S*>(p.f[field]) + go, PS::pack(v), a0, a1);
+                const P sv = g.sr ? SR<S>::pack(v, mix32(seed ^ (uint32_t)go ^ (0x85ebca6bu * (uint32_t)(field + 1))))
+                                  : PS::pack(v);
+                store_pair<S>(reinterpret_cast<S*>(p.f[field]) + go, sv, a0, a1);
             };
             const float2 p1 = kc(0), p2 = kc(1), g1 = kc(2), g2 = kc(3);
             const float2 g3dq = mul2(mul2(p1, f2(g.c_s3, g.c_s3)), dq);  // S3 = P1 c_s3

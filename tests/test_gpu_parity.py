@@ -250,3 +250,22 @@ def test_auto_picks_tiled_for_storage_kinds(behf_lib):
         s = behf.Solver(40, 30, 30, 5.0, 4e-4, radius=4, precision=prec, cpml_width=5)
         assert s.info()["kernel"] == want, prec
         s.close()
+
+
+@pytest.mark.parametrize("precision", ["f16", "bf16"])
+def test_stochastic_rounding_options(behf_lib, oracle, precision):
+    """Stochastic state rounding and unbiased coefficient rounding keep the FP64 parity bars, are reproducible
+    (same seeds every run), and change the result (they are really applied)."""
+    import behf
+    prob = _problem(n=32, nt=160)
+    ref, _ = oracle.run(prob, "f64")
+    runs = []
+    for sr, cr in ((1, 1), (1, 1), (0, 0)):
+        s = behf.solver_for(prob, precision=precision, state_rounding=sr, coef_rounding=cr)
+        s.run(prob.nt)
+        runs.append(s.seismograms())
+        s.close()
+    errs = _per_field_err(oracle, prob, runs[0], ref)
+    assert max(errs.values()) < TOL[precision], errs
+    np.testing.assert_array_equal(runs[0], runs[1])
+    assert not np.array_equal(runs[0], runs[2])
