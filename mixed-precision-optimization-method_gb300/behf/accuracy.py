@@ -22,9 +22,15 @@ from . import FIELDS, solver_for
 from . import problems
 
 
-def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0, state_rounding: int = 0):
+def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0, state_rounding: int = 0,
+            scale_boost: int = 0):
     half = precision in ("f16", "bf16")
-    s = solver_for(prob, precision, kernel, coef_rounding=coef_rounding if half else 0,
+    scales = None
+    if scale_boost and half:  # the automatic scales times 2^scale_boost
+        s0 = solver_for(prob, precision, kernel)
+        scales = [v * 2.0 ** scale_boost for v in s0.info()["scales"]]
+        s0.close()
+    s = solver_for(prob, precision, kernel, scales=scales, coef_rounding=coef_rounding if half else 0,
                    state_rounding=state_rounding if half else 0)
     t0 = time.perf_counter()
     s.run(prob.nt)
@@ -49,6 +55,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=0, help="grid override (test-sized runs)")
     ap.add_argument("--coef-rounding", type=int, default=0, help="1: unbiased coefficient rounding (16-bit kinds)")
     ap.add_argument("--state-rounding", type=int, default=0, help="1: stochastic rounding of the stored fields")
+    ap.add_argument("--scale-boost", type=int, default=0, help="16-bit kinds: automatic scales times 2^B")
     args = ap.parse_args(argv)
     if args.workload == "layered256":
         prob = problems.layered256(n=args.n or 256, nt=args.steps or 2000)
@@ -60,13 +67,15 @@ def main(argv=None):
         prob = problems.random1024(n=args.n or 1024, nt=args.steps or 1200, medium=False, nrec_side=128)
         ref_prec, others = "f32", ["f16", "bf16"]
     out = {"workload": prob.name, "cells": prob.cells, "steps": prob.nt, "reference": ref_prec, "runs": {},
-           "coef_rounding": args.coef_rounding, "state_rounding": args.state_rounding}
+           "coef_rounding": args.coef_rounding, "state_rounding": args.state_rounding,
+           "scale_boost": args.scale_boost}
     ref, meta = run_one(prob, ref_prec)
     out["runs"][ref_prec] = meta
     comps = np.unique(prob.rec_comp)
     out["peak"] = {FIELDS[c]: float(np.abs(ref[prob.rec_comp == c]).max()) for c in comps}
     for prec in others:
-        seis, meta = run_one(prob, prec, coef_rounding=args.coef_rounding, state_rounding=args.state_rounding)
+        seis, meta = run_one(prob, prec, coef_rounding=args.coef_rounding, state_rounding=args.state_rounding,
+                             scale_boost=args.scale_boost)
         meta["rel_l2"] = {FIELDS[c]: rel_l2(seis[prob.rec_comp == c], ref[prob.rec_comp == c]) for c in comps}
         out["runs"][prec] = meta
     print(json.dumps(out))
