@@ -169,7 +169,7 @@ class Problem:
 
 def auto_scales(mod: np.ndarray, amp: float = 1.0, f0: float = 30.0) -> tuple:
     """The library's automatic storage scales (powers of two), from the moduli and the wavelet:
-    s_sigma = s_p = 1/amp, s_v = s_sigma * max sqrt(rho H) (fast-P impedance), and
+    s_sigma = s_p = 16/amp, s_v = s_sigma * max sqrt(rho H) (fast-P impedance), and
     s_q = s_v * clamp(b_min / (rho_max 2 pi f0), 1, 1e6) so the Darcy flux, which is smaller than v by
     about rho omega / b at low frequency, lands in the same range."""
     rho = np.maximum(mod[0].astype(np.float64), 0)
@@ -178,7 +178,7 @@ def auto_scales(mod: np.ndarray, amp: float = 1.0, f0: float = 30.0) -> tuple:
     zmax = float(np.sqrt(rho * hh).max())
     rmax = float(rho.max())
     pos = c1[c1 > 0]
-    ss = 1.0 / amp
+    ss = 16.0 / amp
     sv = ss * (zmax if zmax > 0 else 1.0)
     kq = float(pos.min()) / (rmax * 2 * np.pi * f0) if pos.size and rmax > 0 else 1.0
     kq = min(max(kq, 1.0), 1e6)

@@ -424,7 +424,9 @@ behf_status set_medium_dev(behf_ctx* c, const float* const mod[kNMod]) {
         std::memcpy(&bmin, &r[2], 8);
         const double amp = c->grid.src_amp_hint > 0 ? c->grid.src_amp_hint : 1.0;
         const double f0 = c->grid.src_f0_hint > 0 ? c->grid.src_f0_hint : 30.0;
-        const double ss = 1.0 / amp;
+        // the wavelet peak lands at 2^4 in storage units: fields near the source stay far below the FP16 maximum
+        // (measured: 2^11 saturates an explosive source) while the far field moves up out of the subnormals
+        const double ss = 16.0 / amp;
         const double sv = ss * (zmax > 0 ? zmax : 1.0);
         double kq = (bmin < big && rmax > 0) ? bmin / (rmax * 2.0 * M_PI * f0) : 1.0;
         kq = std::fmin(std::fmax(kq, 1.0), 1e6);
