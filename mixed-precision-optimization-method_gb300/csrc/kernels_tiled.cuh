@@ -107,12 +107,10 @@ constexpr int al128(int b) { return (b + 127) & ~127; }
 struct VMaps {
     CUtensorMap halo[6];  // txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY)
     CUtensorMap zlead[4]; // tzz txz tyz p: own-cell boxes for the z ring
-    CUtensorMap own[18];  // own-cell boxes: vx vy vz qx qy qz, VW1 x y z (FP32), VW3 x y z, VU1 x y z, VU2 x y z
 };
 struct TMaps {
     CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
     CUtensorMap zlead[4]; // vx vy vz qz: own-cell boxes for the z ring
-    CUtensorMap own[14];  // own-cell boxes: sxx syy szz sxy sxz syz p, P1 P2 S1 S2 Sxy Sxz Syz
 };
 
 // ------------------------------------------------------------------------------------- PTX helpers

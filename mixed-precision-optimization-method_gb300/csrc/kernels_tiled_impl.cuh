@@ -24,11 +24,6 @@ namespace tiled {
 #ifndef BEHF_TILED_MINB32
 #define BEHF_TILED_MINB32 1
 #endif
-// 1: each cell's own data (previous fields, coefficients) also arrives by TMA in the pipeline stages; 0: the
-// threads load it from global memory themselves.
-#ifndef BEHF_TILED_OWN
-#define BEHF_TILED_OWN 0
-#endif
 // Longest z range a CTA marches by default (BEHF_OPT_ZCHUNK overrides it).
 #ifndef BEHF_TILED_ZCHUNK
 #define BEHF_TILED_ZCHUNK 64
@@ -57,20 +52,10 @@ struct Map {
                                                                                        : 2 * X + 2 * Y + XY)
                    : (i < 3 ? i * XY : i == 3 ? 3 * XY : 3 * XY + X);
     }
-    static constexpr int hbytes = VEL ? 2 * X + 2 * Y + 2 * XY : 3 * XY + X + Y;
-    // own-cell boxes in the stage (BEHF_TILED_OWN): NOS of the storage type, NOW of FP32 (VW1), NOK coefficient
-    static constexpr int NOS = VEL ? 6 : 7, NOW = VEL ? 3 : 0, NOK = VEL ? 9 : 7;
-    static constexpr int OWW = al128(G::WOWN_B), OWK = al128(G::KOWN_B);
-    static constexpr int obytes = BEHF_TILED_OWN ? NOS * OW + NOW * OWW + NOK * OWK : 0;
-    __host__ __device__ static constexpr int own(int i) {
-        return hbytes + (i < NOS ? i * OW : i < NOS + NOW ? NOS * OW + (i - NOS) * OWW
-                                                          : NOS * OW + NOW * OWW + (i - NOS - NOW) * OWK);
-    }
-    static constexpr int stage = hbytes + obytes;
+    static constexpr int stage = VEL ? 2 * X + 2 * Y + 2 * XY : 3 * XY + X + Y;
     static constexpr int ring = NS * stage;            // z ring: [field][slot] boxes of OW bytes
     static constexpr int bytes = ring + 4 * ZS * OW;
-    static constexpr uint32_t stage_tx = (VEL ? 2 * (G::X_B + G::Y_B + G::XY_B) : 3 * G::XY_B + G::X_B + G::Y_B) +
-                                         (BEHF_TILED_OWN ? NOS * G::OWN_B + NOW * G::WOWN_B + NOK * G::KOWN_B : 0);
+    static constexpr uint32_t stage_tx = VEL ? 2 * (G::X_B + G::Y_B + G::XY_B) : 3 * G::XY_B + G::X_B + G::Y_B;
 };
 
 __device__ __forceinline__ float comp(float2 v, int c) { return c ? v.y : v.x; }
@@ -278,8 +263,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         tma3(b + M::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // txz  (x halo)
         tma3(b + M::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // tyz  (y halo)
         tma3(b + M::halo(5), &maps.halo[5], br, x0 - G::HX, y0 - R, k);  // p    (x, y halo)
-        if (BEHF_TILED_OWN)
-            for (int i = 0; i < 18; i++) tma3(b + M::own(i), &maps.own[i], br, x0, y0, k);
         const int z0 = warm ? k - R : k + R;
         for (int z = z0; z <= k + R; z++)
 #pragma unroll
@@ -303,7 +286,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         P vo_s[3], qo_s[3];
         float2 vw1[3];
         KP kw3[3], ku1[3], ku2[3];
-        if (!BEHF_TILED_OWN && live) {
+        if (live) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
@@ -325,17 +308,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         if (tid == 0) pp.pend[st]--;
         const unsigned char* b = smem + st * M::stage;
         if (live) {
-            if (BEHF_TILED_OWN) {
-#pragma unroll
-                for (int a = 0; a < 3; a++) {
-                    vo_s[a] = *reinterpret_cast<const P*>(b + M::own(a) + oe * sizeof(S));
-                    qo_s[a] = *reinterpret_cast<const P*>(b + M::own(3 + a) + oe * sizeof(S));
-                    vw1[a] = *reinterpret_cast<const float2*>(b + M::own(6 + a) + oe * 4);
-                    kw3[a] = *reinterpret_cast<const KP*>(b + M::own(9 + a) + oe * sizeof(K));
-                    ku1[a] = *reinterpret_cast<const KP*>(b + M::own(12 + a) + oe * sizeof(K));
-                    ku2[a] = *reinterpret_cast<const KP*>(b + M::own(15 + a) + oe * sizeof(K));
-                }
-            }
             const S* txx = reinterpret_cast<const S*>(b + M::halo(0));
             const S* tyy = reinterpret_cast<const S*>(b + M::halo(1));
             const S* txy = reinterpret_cast<const S*>(b + M::halo(2));
@@ -462,8 +434,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
         tma3(b + M::halo(3), &maps.halo[3], br, x0 - G::HX, y0, k);      // qx (x halo)
         tma3(b + M::halo(4), &maps.halo[4], br, x0, y0 - R, k);          // qy (y halo)
-        if (BEHF_TILED_OWN)
-            for (int i = 0; i < 14; i++) tma3(b + M::own(i), &maps.own[i], br, x0, y0, k);
         const int z0 = warm ? k - R : k + R;
         for (int z = z0; z <= k + R; z++)
 #pragma unroll
@@ -486,7 +456,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         const long long go = (long long)k * g.plane + col;
         P so_s[7];
         KP kk[7];
-        if (!BEHF_TILED_OWN && live) {
+        if (live) {
 #pragma unroll
             for (int q = 0; q < 7; q++) {
                 so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
@@ -505,13 +475,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         if (tid == 0) pp.pend[st]--;
         const unsigned char* b = smem + st * M::stage;
         if (live) {
-            if (BEHF_TILED_OWN) {
-#pragma unroll
-                for (int q = 0; q < 7; q++) {
-                    so_s[q] = *reinterpret_cast<const P*>(b + M::own(q) + oe * sizeof(S));
-                    kk[q] = *reinterpret_cast<const KP*>(b + M::own(7 + q) + oe * sizeof(K));
-                }
-            }
             const S* vx = reinterpret_cast<const S*>(b + M::halo(0));
             const S* vy = reinterpret_cast<const S*>(b + M::halo(1));
             const S* vz = reinterpret_cast<const S*>(b + M::halo(2));
@@ -650,15 +613,6 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     ok &= encode<S>(&tm->zlead[1], g, p.f[BEHF_VY], TXC, TY);
     ok &= encode<S>(&tm->zlead[2], g, p.f[BEHF_VZ], TXC, TY);
     ok &= encode<S>(&tm->zlead[3], g, p.f[BEHF_QZ], TXC, TY);
-    typedef typename Traits<S>::K K;
-    typedef typename Traits<S>::W W;
-    for (int i = 0; i < 6; i++) ok &= encode<S>(&vm->own[i], g, p.f[BEHF_VX + i], TXC, TY);
-    for (int i = 0; i < 3; i++) ok &= encode<W>(&vm->own[6 + i], g, p.k[VW1X + i], TXC, TY);
-    const int vk[9] = {VW3X, VW3Y, VW3Z, VU1X, VU1Y, VU1Z, VU2X, VU2Y, VU2Z};
-    for (int i = 0; i < 9; i++) ok &= encode<K>(&vm->own[9 + i], g, p.k[vk[i]], TXC, TY);
-    for (int i = 0; i < 7; i++) ok &= encode<S>(&tm->own[i], g, p.f[BEHF_SXX + i], TXC, TY);
-    const int tk[7] = {P1, P2, S1, S2, SXYC, SXZC, SYZC};
-    for (int i = 0; i < 7; i++) ok &= encode<K>(&tm->own[7 + i], g, p.k[tk[i]], TXC, TY);
     return ok;
 }
 

@@ -27,7 +27,11 @@ def _run(prob, precision, split=None):
 
 
 def test_random1024_fp16_vs_fp32_and_split(behf_lib):
-    prob = problems.random1024(n=1024, nt=400, medium=False, nrec_side=64)
+    prob = problems.random1024(n=1024, nt=400, medium=False, nrec_side=2)
+    # receivers 40 cells (200 m) above the source, so the main pulse reaches them within the 400 steps
+    sx, sy, sz = prob.src
+    xs = np.linspace(100, 924, 128).round().astype(int)
+    prob.rec_ijk, prob.rec_comp = problems.line_receivers(xs, sy, sz - 40, [2, 12])
     a, ok16 = _run(prob, "f16")
     b, ok32 = _run(prob, "f32")
     assert ok16 and ok32
