@@ -194,6 +194,18 @@ struct G25 {
     }
 };
 
+// Asynchronous global -> shared copies (cp.async, no registers held): `valid` 0 writes zero instead.
+__device__ __forceinline__ uint32_t sh_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src, int valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sh_u32(dst)), "l"(src), "n"(BYTES),
+                 "r"(valid ? BYTES : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // KIND 0: T^T gather (X: T0 s4, T4 s6h, T5 s7h, T3 s5;  Y: T1 s4, T4 s6h, T6 s7h, T3 s5;
 //                      Z: T2 s4, T5 s6h, T6 s7h, T3 s5), then V^T per cell.
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
@@ -203,8 +215,11 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
     typedef G25<S, R> W;
     typedef Adj<S, R> Q;
     typedef typename W::A A;
-    __shared__ A shx[4][GY][W::XW];
-    __shared__ A shy[4][W::YH][GX];
+    // NB plane buffers: while plane k is computed from one, the copies of plane k+1 land in the other (one buffer
+    // for FP64, whose two would not fit the static shared-memory limit)
+    constexpr int NB = sizeof(A) == 4 ? 2 : 1;
+    __shared__ A shx[NB][4][GY][W::XW];
+    __shared__ A shy[NB][4][W::YH][GX];
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * GX + tx;
     const int i0 = R + blockIdx.x * GX, j0 = R + blockIdx.y * GY;
     const int i = i0 + tx, j = j0 + ty;
@@ -222,62 +237,75 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
     }
     const long long sy = g.px, sz = g.plane;
     constexpr int NXE = 4 * GY * W::XW, NYE = 4 * W::YH * GX, NT = GX * GY;
-    constexpr int IX = (NXE + NT - 1) / NT, IY = (NYE + NT - 1) / NT;
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
-    for (int k = kb; k < ke; k++) {
-        {  // every load of the plane in flight together, then (near a slab) the corrections, then the stores
-            A v[IX];
-#pragma unroll
-            for (int u = 0; u < IX; u++) {
-                const int e = t + u * NT;
-                const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
-                if (e < NXE) v[u] = W::template corr<false>(g, p, a, ss.arr[0][q], 0, 0, 0, i0 - R + cc, j0 + r, k);
-            }
-            if (cx) {
-#pragma unroll
-                for (int u = 0; u < IX; u++) {
-                    const int e = t + u * NT;
-                    const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
-                    if (e < NXE) v[u] = W::fix(g, p, a, v[u], 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < IX; u++)
-                if (t + u * NT < NXE) (&shx[0][0][0])[t + u * NT] = v[u];
+    // copies of the x and y windows of plane kk into buffer bf (zero outside the grid)
+    auto issue = [&](int kk, int bf) {
+        for (int e = t; e < NXE; e += NT) {
+            const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
+            const int x = i0 - R + cc, y = j0 + r;
+            const bool in = x < g.nx && y < g.ny;
+            const A* src = reinterpret_cast<const A*>(ss.arr[0][q]) +
+                           (in ? (long long)kk * g.plane + (long long)y * g.px + x : 0);
+            cp_async<sizeof(A)>(&shx[bf][0][0][0] + e, src, in);
         }
-        {
-            A v[IY];
+        for (int e = t; e < NYE; e += NT) {
+            const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
+            const int x = i0 + cc, y = j0 - R + r;
+            const bool in = x < g.nx && y < g.ny;
+            const A* src = reinterpret_cast<const A*>(ss.arr[1][q]) +
+                           (in ? (long long)kk * g.plane + (long long)y * g.px + x : 0);
+            cp_async<sizeof(A)>(&shy[bf][0][0][0] + e, src, in);
+        }
+        cp_async_commit();
+    };
+    A zn[4];  // z-queue values of the next plane, loaded one plane ahead
+    if (valid) {
 #pragma unroll
-            for (int u = 0; u < IY; u++) {
-                const int e = t + u * NT;
-                const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
-                if (e < NYE) v[u] = W::template corr<false>(g, p, a, ss.arr[1][q], 1, 0, 0, i0 + cc, j0 - R + r, k);
-            }
-            if (cy) {
-#pragma unroll
-                for (int u = 0; u < IY; u++) {
-                    const int e = t + u * NT;
-                    const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
-                    if (e < NYE) v[u] = W::fix(g, p, a, v[u], 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < IY; u++)
-                if (t + u * NT < NYE) (&shy[0][0][0])[t + u * NT] = v[u];
+        for (int q = 0; q < 4; q++)
+            zn[q] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, kb + R);
+    }
+    issue(kb, 0);
+    for (int k = kb; k < ke; k++) {
+        const int bf = NB == 2 ? ((k - kb) & 1) : 0;
+        if (NB == 2 && k + 1 < ke) {
+            issue(k + 1, bf ^ 1);  // the other buffer was released by the barrier that ended plane k - 1
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         if (valid) {
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                zq[q][2 * R] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
-                                                      k + R);
+            for (int q = 0; q < 4; q++) zq[q][2 * R] = zn[q];
+            if (k + 1 < ke) {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    zn[q] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
+                                                   k + 1 + R);
+            }
+        }
+        __syncthreads();
+        if (cx || cy) {  // CPML corrections of the copied windows near a slab, then a barrier before use
+            if (cx)
+                for (int e = t; e < NXE; e += NT) {
+                    const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
+                    A* d = &shx[bf][0][0][0] + e;
+                    *d = W::fix(g, p, a, *d, 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
+                }
+            if (cy)
+                for (int e = t; e < NYE; e += NT) {
+                    const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
+                    A* d = &shy[bf][0][0][0] + e;
+                    *d = W::fix(g, p, a, *d, 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
+                }
+            __syncthreads();
         }
         __syncthreads();
         if (valid) {
             const long long c = k * sz + j * sy + i;
-#define WX(q) [&](int d) { return shx[q][ty][tx + R + d]; }
-#define WY(q) [&](int d) { return shy[q][ty + R + d][tx]; }
+#define WX(q) [&](int d) { return shx[bf][q][ty][tx + R + d]; }
+#define WY(q) [&](int d) { return shy[bf][q][ty + R + d][tx]; }
 #define WZ(q) [&](int d) { return zq[q][R + d]; }
             if (KIND == 0) {
                 A dl[6];
@@ -388,6 +416,7 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
 #undef WZ
         }
         __syncthreads();
+        if (NB == 1 && k + 1 < ke) issue(k + 1, 0);
         if (valid) {
 #pragma unroll
             for (int q = 0; q < 4; q++)
