@@ -236,27 +236,34 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
                                                   kb - R + d);
     }
     const long long sy = g.px, sz = g.plane;
-    constexpr int NXE = 4 * GY * W::XW, NYE = 4 * W::YH * GX, NT = GX * GY;
+    static_assert(W::XW <= 64 && W::YH <= 16, "window wider than two passes of the block");
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
-    // copies of the x and y windows of plane kk into buffer bf (zero outside the grid)
+    // copies of the x and y windows of plane kk into buffer bf (zero outside the grid).  Warp ty stages row ty of
+    // the x window (columns tx and tx + 32 < XW) and rows ty, ty + 8 < YH of the y window (column tx).
     auto issue = [&](int kk, int bf) {
-        for (int e = t; e < NXE; e += NT) {
-            const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
-            const int x = i0 - R + cc, y = j0 + r;
-            const bool in = x < g.nx && y < g.ny;
-            const A* src = reinterpret_cast<const A*>(ss.arr[0][q]) +
-                           (in ? (long long)kk * g.plane + (long long)y * g.px + x : 0);
-            cp_async<sizeof(A)>(&shx[bf][0][0][0] + e, src, in);
-        }
-        for (int e = t; e < NYE; e += NT) {
-            const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
-            const int x = i0 + cc, y = j0 - R + r;
-            const bool in = x < g.nx && y < g.ny;
-            const A* src = reinterpret_cast<const A*>(ss.arr[1][q]) +
-                           (in ? (long long)kk * g.plane + (long long)y * g.px + x : 0);
-            cp_async<sizeof(A)>(&shy[bf][0][0][0] + e, src, in);
+        const long long pk = (long long)kk * g.plane;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int cc = tx + 32 * h;
+            if (cc < W::XW) {
+                const int x = i0 - R + cc, y = j0 + ty;
+                const bool in = x < g.nx && y < g.ny;
+                const long long off = in ? pk + (long long)y * g.px + x : 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    cp_async<sizeof(A)>(&shx[bf][q][ty][cc], reinterpret_cast<const A*>(ss.arr[0][q]) + off, in);
+            }
+            const int r = ty + 8 * h;
+            if (r < W::YH) {
+                const int x = i0 + tx, y = j0 - R + r;
+                const bool in = x < g.nx && y < g.ny;
+                const long long off = in ? pk + (long long)y * g.px + x : 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    cp_async<sizeof(A)>(&shy[bf][q][r][tx], reinterpret_cast<const A*>(ss.arr[1][q]) + off, in);
+            }
         }
         cp_async_commit();
     };
@@ -287,18 +294,22 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
         }
         __syncthreads();
         if (cx || cy) {  // CPML corrections of the copied windows near a slab, then a barrier before use
-            if (cx)
-                for (int e = t; e < NXE; e += NT) {
-                    const int q = e / (GY * W::XW), r = (e / W::XW) % GY, cc = e % W::XW;
-                    A* d = &shx[bf][0][0][0] + e;
-                    *d = W::fix(g, p, a, *d, 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + r, k);
-                }
-            if (cy)
-                for (int e = t; e < NYE; e += NT) {
-                    const int q = e / (W::YH * GX), r = (e / GX) % W::YH, cc = e % GX;
-                    A* d = &shy[bf][0][0][0] + e;
-                    *d = W::fix(g, p, a, *d, 1, ss.slot[1][q], ss.half[1][q], i0 + cc, j0 - R + r, k);
-                }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int cc = tx + 32 * h, r = ty + 8 * h;
+                if (cx && cc < W::XW)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        A* d = &shx[bf][q][ty][cc];
+                        *d = W::fix(g, p, a, *d, 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + ty, k);
+                    }
+                if (cy && r < W::YH)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        A* d = &shy[bf][q][r][tx];
+                        *d = W::fix(g, p, a, *d, 1, ss.slot[1][q], ss.half[1][q], i0 + tx, j0 - R + r, k);
+                    }
+            }
             __syncthreads();
         }
         __syncthreads();
