@@ -15,6 +15,11 @@ namespace tiled {
 #ifndef BEHF_TILED_NS16
 #define BEHF_TILED_NS16 2
 #endif
+// 16-bit kinds: the velocity kernel keeps 2 CTAs per SM (at 3 its register cap of 80 spills and it slows
+// down), the stress kernel runs 3 (80 registers without spills; measured 17.5 -> 16.2 ms at 1024^3 FP16).
+#ifndef BEHF_TILED_MINB16_T
+#define BEHF_TILED_MINB16_T 3
+#endif
 #ifndef BEHF_TILED_MINB16
 #define BEHF_TILED_MINB16 2
 #endif
@@ -31,6 +36,7 @@ namespace tiled {
 template <class S> struct Depth {
     static constexpr int NS = sizeof(S) == 2 ? BEHF_TILED_NS16 : BEHF_TILED_NS32;
     static constexpr int MINB = sizeof(S) == 2 ? BEHF_TILED_MINB16 : BEHF_TILED_MINB32;
+    static constexpr int MINB_T = sizeof(S) == 2 ? BEHF_TILED_MINB16_T : BEHF_TILED_MINB32;
 };
 constexpr int NWARP = NTH / 32;
 
@@ -390,7 +396,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
 
 // ----------------------------------------------------------------------------------------- stress
 template <class S, int R>
-__global__ void __launch_bounds__(NTH, Depth<S>::MINB)
+__global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
     k_str(const __grid_constant__ TMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
     typedef Pair<S> PS;
     typedef typename PS::T P;
@@ -632,7 +638,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     const int nbx = (g.nx - R + TXC - 1) / TXC, nby = (g.ny - R + TY - 1) / TY;
     const int planes = g.nz - 2 * R;
     // enough CTAs for every SM: split z into chunks when the xy tiling alone is too small
-    const int target = 2 * Depth<S>::MINB * num_sms();
+    const int target = 2 * (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
     int nzc = (target + nbx * nby - 1) / (nbx * nby);
     nzc = nzc < 1 ? 1 : nzc;
     const int maxc = planes / 16 > 1 ? planes / 16 : 1;
