@@ -15,19 +15,25 @@ namespace tiled {
 #ifndef BEHF_TILED_NS16
 #define BEHF_TILED_NS16 2
 #endif
-// 16-bit kinds: the velocity kernel keeps 2 CTAs per SM (at 3 its register cap of 80 spills and it slows
-// down), the stress kernel runs 3 (80 registers without spills; measured 17.5 -> 16.2 ms at 1024^3 FP16).
+// 16-bit kinds run 3 CTAs per SM (80 registers: 6 warps per scheduler instead of 4; measured at 1024^3 FP16
+// stress 17.5 -> 16.2 ms, velocity 18.35 -> 17.8 ms with its own-cell loads issued after the stencils).
 #ifndef BEHF_TILED_MINB16_T
 #define BEHF_TILED_MINB16_T 3
 #endif
 #ifndef BEHF_TILED_MINB16
-#define BEHF_TILED_MINB16 2
+#define BEHF_TILED_MINB16 3
 #endif
 #ifndef BEHF_TILED_NS32
 #define BEHF_TILED_NS32 2
 #endif
 #ifndef BEHF_TILED_MINB32
 #define BEHF_TILED_MINB32 1
+#endif
+// Velocity kernel, 16-bit kinds: 1 issues the cell's own loads before the pipeline waits (their latency overlaps
+// the waits, but 21 more registers stay live), 0 after the stencils (fits 80 registers; the best choice at 3 CTAs
+// per SM).  FP32 (1 CTA per SM) always issues them early.
+#ifndef BEHF_TILED_VLOAD_EARLY16
+#define BEHF_TILED_VLOAD_EARLY16 0
 #endif
 // Longest z range a CTA marches by default (BEHF_OPT_ZCHUNK overrides it).
 #ifndef BEHF_TILED_ZCHUNK
@@ -286,13 +292,13 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
     bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it % NS;
-        // the cell's own data of plane k (v, q, VW1 in FP32, VW3, VU1, VU2) does not go through the pipeline:
-        // its loads are issued before the waits so that their latency overlaps them and the stencils
+        // the cell's own data of plane k (v, q, VW1 in FP32, VW3, VU1, VU2) does not go through the pipeline: its
+        // coalesced pair loads are issued before the waits (FP32) or after the stencils (16-bit kinds)
         const long long go = (long long)k * g.plane + col;
         P vo_s[3], qo_s[3];
         float2 vw1[3];
         KP kw3[3], ku1[3], ku2[3];
-        if (live) {
+        auto load_own = [&]() {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
@@ -302,7 +308,9 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
                 ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
                 ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
             }
-        }
+        };
+        constexpr bool early = sizeof(S) == 4 || BEHF_TILED_VLOAD_EARLY16;
+        if (early && live) load_own();
         bool ok = true;
         if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
         if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
@@ -365,6 +373,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
+            if (!early) load_own();
             auto km = [&](KP kv, int j) { return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j])); };
 #pragma unroll
             for (int a = 0; a < 3; a++) {
