@@ -42,7 +42,7 @@ UNIT = "Gpt/s"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the tiled radius-4 FP16
 # kernels on this workload at 1024^3, from one ncu capture (one pass per launch), per updated cell; the
 # bench multiplies by the cells of its own grid.
-NCU_BYTES_PER_CELL = {("f16", "velocity"): 78.35, ("f16", "stress"): 63.00}
+NCU_BYTES_PER_CELL = {("f16", "velocity"): 82.01, ("f16", "stress"): 66.68}
 NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1024^3 launch, per cell x cells"
 
 
