@@ -62,16 +62,54 @@ struct Adj {
     }
     static __device__ __forceinline__ A prof(const void* v, int i) { return reinterpret_cast<const A*>(v)[i]; }
 
-    // adjoint CPML memory update of one slot
-    static __device__ __forceinline__ void lmem(const Geom& g, const DevPtrs& p, const AdjPtrs& a, A lD, int ax,
-                                                int slot, bool half, int pos, long long so) {
-        const A Ap = half ? prof(p.pa2[ax], pos) : prof(p.pa[ax], pos);
-        const A B = half ? prof(p.pb2[ax], pos) : prof(p.pb[ax], pos);
-        A* ps = reinterpret_cast<A*>(a.lpsi[ax][slot]) + so;
-        A* pv = reinterpret_cast<A*>(a.lprv[ax][slot]) + so;
-        const A Lm = *ps + lD;
-        *ps = Ap * Lm;
-        *pv = Ap * B * Lm;
+};
+
+// Adjoint CPML memory update  lpsi = A (lpsi + lD),  lprv = A B (lpsi_old + lD)  of the four slots SB..SB+3 on
+// every slab axis of one cell, split into a load phase and a store phase so that a kernel can issue all of a
+// cell's loads before its first store.  Bit q of H set: slot SB+q uses the half-shifted profiles.
+template <class A, int SB, int H>
+struct MemUpd {
+    A L[3][4], pa[3], pb[3];
+    long long so[3];
+    int s[3];
+    __device__ __forceinline__ void load(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int i, int j, int k) {
+        s[0] = slab_index(i, g.nx, g.L);
+        s[1] = slab_index(j, g.ny, g.L);
+        s[2] = slab_index(k, g.nz, g.L);
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            if (s[ax] < 0) continue;
+            const int pos = ax == 0 ? i : ax == 1 ? j : k;
+            so[ax] = slab_off(g, ax, i, j, k, s[ax]);
+            pa[ax] = reinterpret_cast<const A*>(p.pa[ax])[pos];
+            pb[ax] = reinterpret_cast<const A*>(p.pb[ax])[pos];
+#pragma unroll
+            for (int q = 0; q < 4; q++) L[ax][q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[so[ax]];
+        }
+        if (H != 0) {  // the half-shifted profiles replace pa, pb for the flagged slots
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+                if (s[ax] < 0) continue;
+                const int pos = ax == 0 ? i : ax == 1 ? j : k;
+                pa2_[ax] = reinterpret_cast<const A*>(p.pa2[ax])[pos];
+                pb2_[ax] = reinterpret_cast<const A*>(p.pb2[ax])[pos];
+            }
+        }
+    }
+    A pa2_[3], pb2_[3];
+    __device__ __forceinline__ void store(const AdjPtrs& a, const A (&D)[3][4]) const {
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            if (s[ax] < 0) continue;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const bool h = (H >> q) & 1;
+                const A Ap = h ? pa2_[ax] : pa[ax], B = h ? pb2_[ax] : pb[ax];
+                const A Lm = L[ax][q] + D[ax][q];
+                reinterpret_cast<A*>(a.lpsi[ax][SB + q])[so[ax]] = Ap * Lm;
+                reinterpret_cast<A*>(a.lprv[ax][SB + q])[so[ax]] = Ap * B * Lm;
+            }
+        }
     }
 };
 
@@ -96,43 +134,78 @@ struct Adj {
 // A gather reads the adjoint memory of its own slots only, and each memory update runs after every gather
 // that reads those slots.
 template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
+__global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a, int first) {
     typedef Adj<S, R> Q;
     typedef typename Q::A A;
     CELL_INDEX
-    const A lp = Q::ad(a.lf[BEHF_P])[c], lxx = Q::ad(a.lf[BEHF_SXX])[c], lyy = Q::ad(a.lf[BEHF_SYY])[c];
-    const A lzz = Q::ad(a.lf[BEHF_SZZ])[c], lxy = Q::ad(a.lf[BEHF_SXY])[c], lxz = Q::ad(a.lf[BEHF_SXZ])[c];
-    const A lyz = Q::ad(a.lf[BEHF_SYZ])[c];
-    const A p1 = Q::coef(g, p, P1, c), p2 = Q::coef(g, p, P2, c);
-    const A s1 = Q::coef(g, p, S1, c), s2 = Q::coef(g, p, S2, c), s3 = Q::coef(g, p, S3, c);
+    // Every load of the cell is issued before its first store: the arrays never alias, but the compiler cannot
+    // know that, and each store between two loads would cost one memory round trip.
+    A lt[7];  // 0 sxx, 1 syy, 2 szz, 3 sxy, 4 sxz, 5 syz, 6 p
+#pragma unroll
+    for (int q = 0; q < 7; q++) lt[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
+    A kc[8];  // P1, P2, S1, S2, S3, SXYC, SXZC, SYZC
+#pragma unroll
+    for (int q = 0; q < 8; q++) kc[q] = Q::coef(g, p, P1 + q, c);
+    const bool slab = !interior(g, i, j, k);
+    const bool gr = a.grad && !slab;
+    A du[10], go[8];
+    if (gr) {
+        du[0] = Q::bwd(a.cur[BEHF_VX], c, 1);   // uxx
+        du[1] = Q::bwd(a.cur[BEHF_VY], c, sy);  // uyy
+        du[2] = Q::bwd(a.cur[BEHF_VZ], c, sz);  // uzz
+        du[3] = Q::bwd(a.cur[BEHF_QX], c, 1) + Q::bwd(a.cur[BEHF_QY], c, sy) + Q::bwd(a.cur[BEHF_QZ], c, sz);
+        du[4] = Q::fwd(a.cur[BEHF_VX], c, sy);  // uxy
+        du[5] = Q::fwd(a.cur[BEHF_VY], c, 1);   // uyx
+        du[6] = Q::fwd(a.cur[BEHF_VX], c, sz);  // uxz
+        du[7] = Q::fwd(a.cur[BEHF_VZ], c, 1);   // uzx
+        du[8] = Q::fwd(a.cur[BEHF_VY], c, sz);  // uyz
+        du[9] = Q::fwd(a.cur[BEHF_VZ], c, sy);  // uzy
+#pragma unroll
+        for (int q = 0; q < 8; q++) go[q] = Q::ad(a.g[P1 + q])[c];
+    }
+    // V-slot adjoint memory of the previous backward step: its tmpV at this cell (read by the V^T gather of that
+    // step, which has completed), on slab cells
+    const bool mem = slab && g.W > 0 && !first;
+    A tv[6];
+    MemUpd<A, 0, 0x3> mv;
+    if (mem) {
+#pragma unroll
+        for (int q = 0; q < 6; q++) tv[q] = Q::ad(a.tmpV[q])[c];
+        mv.load(g, p, a, i, j, k);
+    }
+    const A lp = lt[6], lxx = lt[0], lyy = lt[1], lzz = lt[2];
+    const A p1 = kc[0], p2 = kc[1], s1 = kc[2], s2 = kc[3], s3 = kc[4];
     Q::ad(a.tmpT[0])[c] = -p1 * lp + s2 * lxx + s1 * (lyy + lzz);
     Q::ad(a.tmpT[1])[c] = -p1 * lp + s2 * lyy + s1 * (lxx + lzz);
     Q::ad(a.tmpT[2])[c] = -p1 * lp + s2 * lzz + s1 * (lxx + lyy);
     Q::ad(a.tmpT[3])[c] = -p2 * lp + s3 * (lxx + lyy + lzz);
-    Q::ad(a.tmpT[4])[c] = Q::coef(g, p, SXYC, c) * lxy;
-    Q::ad(a.tmpT[5])[c] = Q::coef(g, p, SXZC, c) * lxz;
-    Q::ad(a.tmpT[6])[c] = Q::coef(g, p, SYZC, c) * lyz;
-    if (a.grad && interior(g, i, j, k)) {
-        const A uxx = Q::bwd(a.cur[BEHF_VX], c, 1), uyy = Q::bwd(a.cur[BEHF_VY], c, sy);
-        const A uzz = Q::bwd(a.cur[BEHF_VZ], c, sz);
-        const A dq = Q::bwd(a.cur[BEHF_QX], c, 1) + Q::bwd(a.cur[BEHF_QY], c, sy) + Q::bwd(a.cur[BEHF_QZ], c, sz);
-        const A uxy = Q::fwd(a.cur[BEHF_VX], c, sy), uyx = Q::fwd(a.cur[BEHF_VY], c, 1);
-        const A uxz = Q::fwd(a.cur[BEHF_VX], c, sz), uzx = Q::fwd(a.cur[BEHF_VZ], c, 1);
-        const A uyz = Q::fwd(a.cur[BEHF_VY], c, sz), uzy = Q::fwd(a.cur[BEHF_VZ], c, sy);
-        Q::ad(a.g[P1])[c] += -lp * (uxx + uyy + uzz);
-        Q::ad(a.g[P2])[c] += -lp * dq;
-        Q::ad(a.g[S1])[c] += lxx * (uyy + uzz) + lyy * (uxx + uzz) + lzz * (uxx + uyy);
-        Q::ad(a.g[S2])[c] += lxx * uxx + lyy * uyy + lzz * uzz;
-        Q::ad(a.g[S3])[c] += (lxx + lyy + lzz) * dq;
-        Q::ad(a.g[SXYC])[c] += lxy * (uxy + uyx);
-        Q::ad(a.g[SXZC])[c] += lxz * (uxz + uzx);
-        Q::ad(a.g[SYZC])[c] += lyz * (uyz + uzy);
+    Q::ad(a.tmpT[4])[c] = kc[5] * lt[3];
+    Q::ad(a.tmpT[5])[c] = kc[6] * lt[4];
+    Q::ad(a.tmpT[6])[c] = kc[7] * lt[5];
+    if (gr) {
+        const A uxx = du[0], uyy = du[1], uzz = du[2], dq = du[3];
+        Q::ad(a.g[P1])[c] = go[0] - lp * (uxx + uyy + uzz);
+        Q::ad(a.g[P2])[c] = go[1] - lp * dq;
+        Q::ad(a.g[S1])[c] = go[2] + lxx * (uyy + uzz) + lyy * (uxx + uzz) + lzz * (uxx + uyy);
+        Q::ad(a.g[S2])[c] = go[3] + lxx * uxx + lyy * uyy + lzz * uzz;
+        Q::ad(a.g[S3])[c] = go[4] + (lxx + lyy + lzz) * dq;
+        Q::ad(a.g[SXYC])[c] = go[5] + lt[3] * (du[4] + du[5]);
+        Q::ad(a.g[SXZC])[c] = go[6] + lt[4] * (du[6] + du[7]);
+        Q::ad(a.g[SYZC])[c] = go[7] + lt[5] * (du[8] + du[9]);
+    }
+    if (mem) {
+        // axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
+        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y
+        const A D[3][4] = {{tv[0], tv[3], tv[1], tv[2]}, {tv[1], tv[4], tv[0], tv[2]}, {tv[2], tv[5], tv[0], tv[1]}};
+        mv.store(a, D);
     }
 }
 
 // Gathers, z-marching: a 32 x 8 block owns an xy tile and walks a z range.  Each gather needs 12 corrected
 // derivative-group adjoints: 4 with x stencils (staged per plane in shared memory with an x halo of R), 4 with
-// y stencils (shared memory, y halo R) and 4 with z stencils (a register queue of 2R+1 planes per thread).
+// y stencils (shared memory, y halo R) and 4 with z stencils (a shared-memory ring of the 2R+2 planes k-R ..
+// k+R+1, each thread reading its own column).  Everything for plane k+1 is copied (cp.async, 16-byte chunks
+// where the tile rows are 16-byte aligned) while plane k is computed.
 // "Corrected" = the adjoint CPML correction of the stencil's own axis and slot applied at the cell it was read
 // from: lD = lD~ + B (lpsi + lD~) + lprev on slab cells, lD~ elsewhere (zero off the updated cells).
 constexpr int GX = 32, GY = 8;
@@ -146,8 +219,6 @@ struct StageSet {
 template <class S, int R>
 struct G25 {
     typedef typename Traits<S>::C A;
-    static constexpr int XW = GX + 2 * R;
-    static constexpr int YH = GY + 2 * R;
     template <bool CHK>
     static __device__ __forceinline__ A corr(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const void* arr,
                                              int ax, int slot, int half, int x, int y, int k) {
@@ -194,168 +265,203 @@ struct G25 {
     }
 };
 
-// Asynchronous global -> shared copies (cp.async, no registers held): `valid` 0 writes zero instead.
+// Asynchronous global -> shared copies (cp.async, no registers held): the first `bytes` bytes come from src,
+// the rest of the BYTES is zero-filled (bytes = 0 reads nothing).
 __device__ __forceinline__ uint32_t sh_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 template <int BYTES>
-__device__ __forceinline__ void cp_async(void* dst, const void* src, int valid) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sh_u32(dst)), "l"(src), "n"(BYTES),
-                 "r"(valid ? BYTES : 0)
+__device__ __forceinline__ void cp_async(void* dst, const void* src, int bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sh_u32(dst)), "l"(src), "n"(BYTES), "r"(bytes)
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Dynamic shared memory of a gather CTA (elements of A): two plane buffers of the x windows [4][GY][XWP] and
+// of the y windows [4][YH][GX], then the z ring [4][ZS][GY * GX].  Rows of the x window start at the 16-byte
+// aligned column i0 - R = 32 bx and are padded to whole 16-byte chunks; y-window and z-ring rows start at
+// i0 = R + 32 bx, 16-byte aligned when R * sizeof(A) is (YV), else copied element by element.
+template <class S, int R>
+struct GMap {
+    typedef typename Traits<S>::C A;
+    static constexpr int CH = 16 / (int)sizeof(A);
+    static constexpr int XW = GX + 2 * R;
+    static constexpr int XWP = (XW + CH - 1) / CH * CH;
+    static constexpr int YH = GY + 2 * R;
+    static constexpr int ZS = 2 * R + 2;
+    static constexpr bool YV = (R * (int)sizeof(A)) % 16 == 0;
+    static constexpr int XB = 4 * GY * XWP, YB = 4 * YH * GX;
+    static constexpr int X_OFF = 0, Y_OFF = 2 * XB, Z_OFF = Y_OFF + 2 * YB;
+    static constexpr int BYTES = (Z_OFF + 4 * ZS * GY * GX) * (int)sizeof(A);
+};
+
 // KIND 0: T^T gather (X: T0 s4, T4 s6h, T5 s7h, T3 s5;  Y: T1 s4, T4 s6h, T6 s7h, T3 s5;
 //                      Z: T2 s4, T5 s6h, T6 s7h, T3 s5), then V^T per cell.
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
 //                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update.
 template <class S, int R, int KIND>
-__global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc, int first) {
+__global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc) {
     typedef G25<S, R> W;
     typedef Adj<S, R> Q;
+    typedef GMap<S, R> M;
     typedef typename W::A A;
-    // NB plane buffers: while plane k is computed from one, the copies of plane k+1 land in the other (one buffer
-    // for FP64, whose two would not fit the static shared-memory limit)
-    constexpr int NB = sizeof(A) == 4 ? 2 : 1;
-    __shared__ A shx[NB][4][GY][W::XW];
-    __shared__ A shy[NB][4][W::YH][GX];
+    extern __shared__ __align__(16) unsigned char gsm_raw[];
+    A* const gsm = reinterpret_cast<A*>(gsm_raw);
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * GX + tx;
     const int i0 = R + blockIdx.x * GX, j0 = R + blockIdx.y * GY;
     const int i = i0 + tx, j = j0 + ty;
     const bool valid = i < g.nx - R && j < g.ny - R;
     const int kb = R + blockIdx.z * zc, ke = min(kb + zc, g.nz - R);
     if (kb >= ke) return;
-    A zq[4][2 * R + 1];
-    if (valid) {
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-#pragma unroll
-            for (int d = 0; d < 2 * R; d++)
-                zq[q][d] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
-                                                  kb - R + d);
-    }
     const long long sy = g.px, sz = g.plane;
-    static_assert(W::XW <= 64 && W::YH <= 16, "window wider than two passes of the block");
+    static_assert(M::YH <= 16 && M::XWP <= 64, "window larger than the block's copy pattern");
+    auto shx = [&](int bf, int q, int r, int col) -> A& { return gsm[M::X_OFF + bf * M::XB + (q * GY + r) * M::XWP + col]; };
+    auto shy = [&](int bf, int q, int r, int col) -> A& { return gsm[M::Y_OFF + bf * M::YB + (q * M::YH + r) * GX + col]; };
+    auto zr = [&](int q, int slot) -> A* { return gsm + M::Z_OFF + (q * M::ZS + slot) * (GY * GX); };
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
-    // copies of the x and y windows of plane kk into buffer bf (zero outside the grid).  Warp ty stages row ty of
-    // the x window (columns tx and tx + 32 < XW) and rows ty, ty + 8 < YH of the y window (column tx).
-    auto issue = [&](int kk, int bf) {
-        const long long pk = (long long)kk * g.plane;
+    // bytes of the 16-byte chunk at column x that lie inside the grid (rows outside it: 0)
+    auto chunk_bytes = [&](int x, int y) {
+        const int n = (g.nx - x) * (int)sizeof(A);
+        return (y >= g.ny || n <= 0) ? 0 : (n < 16 ? n : 16);
+    };
+    // z ring: plane zz of the four z-stencil arrays into its slot (CPML-corrected element by element on a z-slab plane)
+    auto zfill = [&](int zz) {
+        const int slot = zz % M::ZS;
+        const bool zslab = g.W > 0 && slab_index(zz, g.nz, g.L) >= 0;
+        if (zslab || !M::YV) {
+            if (valid) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int cc = tx + 32 * h;
-            if (cc < W::XW) {
-                const int x = i0 - R + cc, y = j0 + ty;
-                const bool in = x < g.nx && y < g.ny;
-                const long long off = in ? pk + (long long)y * g.px + x : 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    cp_async<sizeof(A)>(&shx[bf][q][ty][cc], reinterpret_cast<const A*>(ss.arr[0][q]) + off, in);
+                for (int q = 0; q < 4; q++) {
+                    if (zslab) {
+                        zr(q, slot)[t] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q],
+                                                                i, j, zz);
+                    } else {
+                        cp_async<sizeof(A)>(zr(q, slot) + t,
+                                            reinterpret_cast<const A*>(ss.arr[2][q]) + zz * sz + j * sy + i,
+                                            (int)sizeof(A));
+                    }
+                }
             }
-            const int r = ty + 8 * h;
-            if (r < W::YH) {
-                const int x = i0 + tx, y = j0 - R + r;
-                const bool in = x < g.nx && y < g.ny;
-                const long long off = in ? pk + (long long)y * g.px + x : 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    cp_async<sizeof(A)>(&shy[bf][q][r][tx], reinterpret_cast<const A*>(ss.arr[1][q]) + off, in);
+        } else {
+            // warp ty copies row ty: (array, chunk) pairs over the lanes
+            constexpr int NCH = GX / M::CH;
+            for (int u = tx; u < 4 * NCH; u += 32) {
+                const int q = u / NCH, ch = u % NCH;
+                const int x = i0 + ch * M::CH, y = j;
+                const int nb = chunk_bytes(x, y);
+                const long long off = nb ? zz * sz + (long long)y * sy + x : 0;
+                cp_async<16>(zr(q, slot) + ty * GX + ch * M::CH, reinterpret_cast<const A*>(ss.arr[2][q]) + off, nb);
             }
         }
-        cp_async_commit();
     };
-    A zn[4];  // z-queue values of the next plane, loaded one plane ahead
-    if (valid) {
+    // x and y windows of plane kk into buffer bf (zero outside the grid)
+    auto issue = [&](int kk, int bf) {
+        const long long pk = (long long)kk * sz;
+        {  // x window: warp ty copies row ty, 16-byte chunks
+            constexpr int NCH = M::XWP / M::CH;
+            const int y = j0 + ty;
+            for (int u = tx; u < 4 * NCH; u += 32) {
+                const int q = u / NCH, ch = u % NCH;
+                const int x = i0 - R + ch * M::CH;
+                const int nb = chunk_bytes(x, y);
+                const long long off = nb ? pk + (long long)y * sy + x : 0;
+                cp_async<16>(&shx(bf, q, ty, ch * M::CH), reinterpret_cast<const A*>(ss.arr[0][q]) + off, nb);
+            }
+        }
+        if (M::YV) {  // y window: the YH rows x 4 arrays x (GX / CH) chunks over the block
+            constexpr int NCH = GX / M::CH;
+            for (int u = t; u < M::YH * 4 * NCH; u += GX * GY) {
+                const int ch = u % NCH, rq = u / NCH, q = rq % 4, r = rq / 4;
+                const int x = i0 + ch * M::CH, y = j0 - R + r;
+                const int nb = chunk_bytes(x, y);
+                const long long off = nb ? pk + (long long)y * sy + x : 0;
+                cp_async<16>(&shy(bf, q, r, ch * M::CH), reinterpret_cast<const A*>(ss.arr[1][q]) + off, nb);
+            }
+        } else {
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            zn[q] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j, kb + R);
-    }
+            for (int h = 0; h < 2; h++) {
+                const int r = ty + 8 * h;
+                if (r < M::YH) {
+                    const int x = i0 + tx, y = j0 - R + r;
+                    const bool in = x < g.nx && y < g.ny;
+                    const long long off = in ? pk + (long long)y * sy + x : 0;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        cp_async<sizeof(A)>(&shy(bf, q, r, tx), reinterpret_cast<const A*>(ss.arr[1][q]) + off,
+                                            in ? (int)sizeof(A) : 0);
+                }
+            }
+        }
+    };
+    for (int zz = kb - R; zz <= kb + R; zz++) zfill(zz);
     issue(kb, 0);
+    cp_async_commit();
     for (int k = kb; k < ke; k++) {
-        const int bf = NB == 2 ? ((k - kb) & 1) : 0;
-        if (NB == 2 && k + 1 < ke) {
-            issue(k + 1, bf ^ 1);  // the other buffer was released by the barrier that ended plane k - 1
+        const int bf = (k - kb) & 1;
+        if (k + 1 < ke) {
+            // the other window buffer and the ring slot of plane k - R - 1 were released by the barrier that ended
+            // plane k - 1
+            issue(k + 1, bf ^ 1);
+            zfill(k + 1 + R);
+            cp_async_commit();
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
         }
-        if (valid) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) zq[q][2 * R] = zn[q];
-            if (k + 1 < ke) {
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    zn[q] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q], i, j,
-                                                   k + 1 + R);
-            }
-        }
         __syncthreads();
-        if (cx || cy) {  // CPML corrections of the copied windows near a slab, then a barrier before use
+        if (cx || cy) {  // CPML corrections of the copied windows near a slab (all loads, then the writes)
+            A fxv[2][4], fyv[2][4];
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int cc = tx + 32 * h, r = ty + 8 * h;
-                if (cx && cc < W::XW)
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        A* d = &shx[bf][q][ty][cc];
-                        *d = W::fix(g, p, a, *d, 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc, j0 + ty, k);
-                    }
-                if (cy && r < W::YH)
+                for (int q = 0; q < 4; q++) {
+                    if (cx && cc < M::XW)
+                        fxv[h][q] = W::fix(g, p, a, shx(bf, q, ty, cc), 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc,
+                                           j0 + ty, k);
+                    if (cy && r < M::YH)
+                        fyv[h][q] = W::fix(g, p, a, shy(bf, q, r, tx), 1, ss.slot[1][q], ss.half[1][q], i0 + tx,
+                                           j0 - R + r, k);
+                }
+            }
+            __syncthreads();  // every thread has read the raw windows
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        A* d = &shy[bf][q][r][tx];
-                        *d = W::fix(g, p, a, *d, 1, ss.slot[1][q], ss.half[1][q], i0 + tx, j0 - R + r, k);
-                    }
+            for (int h = 0; h < 2; h++) {
+                const int cc = tx + 32 * h, r = ty + 8 * h;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (cx && cc < M::XW) shx(bf, q, ty, cc) = fxv[h][q];
+                    if (cy && r < M::YH) shy(bf, q, r, tx) = fyv[h][q];
+                }
             }
             __syncthreads();
         }
-        __syncthreads();
         if (valid) {
             const long long c = k * sz + j * sy + i;
-#define WX(q) [&](int d) { return shx[bf][q][ty][tx + R + d]; }
-#define WY(q) [&](int d) { return shy[bf][q][ty + R + d][tx]; }
-#define WZ(q) [&](int d) { return zq[q][R + d]; }
-            if (KIND == 0) {
-                A dl[6];
-                dl[0] = W::fwd(WX(0)) + W::bwd(WY(1)) + W::bwd(WZ(1));
-                dl[1] = W::fwd(WY(0)) + W::bwd(WX(1)) + W::bwd(WZ(2));
-                dl[2] = W::fwd(WZ(0)) + W::bwd(WX(2)) + W::bwd(WY(2));
-                dl[3] = W::fwd(WX(3));
-                dl[4] = W::fwd(WY(3));
-                dl[5] = W::fwd(WZ(3));
-                const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
-                if (!first && g.W > 0 && (si >= 0 || sj >= 0 || sk >= 0)) {  // V-slot memory of the previous step
-                    A tv[6];
+            int zs[2 * R + 1];  // ring slots of planes k-R .. k+R
 #pragma unroll
-                    for (int q = 0; q < 6; q++) tv[q] = Q::ad(a.tmpV[q])[c];
-                    if (si >= 0) {
-                        const long long so = slab_off(g, 0, i, j, k, si);
-                        Q::lmem(g, p, a, tv[0], 0, 0, true, i, so);
-                        Q::lmem(g, p, a, tv[3], 0, 1, true, i, so);
-                        Q::lmem(g, p, a, tv[1], 0, 2, false, i, so);
-                        Q::lmem(g, p, a, tv[2], 0, 3, false, i, so);
-                    }
-                    if (sj >= 0) {
-                        const long long so = slab_off(g, 1, i, j, k, sj);
-                        Q::lmem(g, p, a, tv[1], 1, 0, true, j, so);
-                        Q::lmem(g, p, a, tv[4], 1, 1, true, j, so);
-                        Q::lmem(g, p, a, tv[0], 1, 2, false, j, so);
-                        Q::lmem(g, p, a, tv[2], 1, 3, false, j, so);
-                    }
-                    if (sk >= 0) {
-                        const long long so = slab_off(g, 2, i, j, k, sk);
-                        Q::lmem(g, p, a, tv[2], 2, 0, true, k, so);
-                        Q::lmem(g, p, a, tv[5], 2, 1, true, k, so);
-                        Q::lmem(g, p, a, tv[0], 2, 2, false, k, so);
-                        Q::lmem(g, p, a, tv[1], 2, 3, false, k, so);
-                    }
-                }
+            for (int d = 0; d <= 2 * R; d++) zs[d] = (k - R + d) % M::ZS;
+#define WX(q) [&](int d) { return shx(bf, q, ty, tx + R + d); }
+#define WY(q) [&](int d) { return shy(bf, q, ty + R + d, tx); }
+#define WZ(q) [&](int d) { return zr(q, zs[R + d])[t]; }
+            // Each cell issues all its global loads before its first global store (see k_adj_a).
+            if (KIND == 0) {
                 // V^T at this cell with lv = lv_old - dl[0..2], lq' = lq_old - dl[3..5]
+                A lvo[3], lqo[3], vu2[3], vw1[3], vu1[3], vw2[3], vw3[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    lvo[d] = Q::ad(a.lf[BEHF_VX + d])[c];
+                    lqo[d] = Q::ad(a.lf[BEHF_QX + d])[c];
+                    vu2[d] = Q::coef(g, p, VU2X + d, c);
+                    vw1[d] = Q::vw1(p, d, c);
+                    vu1[d] = Q::coef(g, p, VU1X + d, c);
+                    vw2[d] = Q::coef(g, p, VW2X + d, c);
+                    vw3[d] = Q::coef(g, p, (d == 2 && g.bug) ? VW3Y : VW3X + d, c);  // reference: vz uses VW3y
+                }
                 const bool gr = a.grad && interior(g, i, j, k);
-                A sum[3] = {0, 0, 0}, dp[3] = {0, 0, 0};
+                A sum[3], dp[3], qo[3], qn[3], go[15];
                 if (gr) {
                     sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) + Q::bwd(a.cur[BEHF_SXZ], c, sz);
                     sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sz);
@@ -363,63 +469,72 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
                     dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
                     dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
                     dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        qo[d] = Q::ls(a.qprev[d], c);
+                        qn[d] = Q::ls(a.cur[BEHF_QX + d], c);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 15; q++) go[q] = Q::ad(a.g[q])[c];
                 }
+                A dl[6];
+                dl[0] = W::fwd(WX(0)) + W::bwd(WY(1)) + W::bwd(WZ(1));
+                dl[1] = W::fwd(WY(0)) + W::bwd(WX(1)) + W::bwd(WZ(2));
+                dl[2] = W::fwd(WZ(0)) + W::bwd(WX(2)) + W::bwd(WY(2));
+                dl[3] = W::fwd(WX(3));
+                dl[4] = W::fwd(WY(3));
+                dl[5] = W::fwd(WZ(3));
+                A mu[3], lv[3];
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    const int vw3 = (d == 2 && g.bug) ? VW3Y : VW3X + d;
-                    A* lvp = Q::ad(a.lf[BEHF_VX + d]) + c;
-                    A* lqp = Q::ad(a.lf[BEHF_QX + d]) + c;
-                    const A lv = *lvp - dl[d], lq = *lqp - dl[3 + d];
-                    const A vu2 = Q::coef(g, p, VU2X + d, c);
-                    const A mu = lq - vu2 * lv;
-                    *lvp = lv;
-                    *lqp = Q::vw1(p, d, c) * mu + vu2 * lv;
-                    Q::ad(a.tmpV[d])[c] = Q::coef(g, p, VU1X + d, c) * lv - Q::coef(g, p, VW2X + d, c) * mu;
-                    Q::ad(a.tmpV[3 + d])[c] = -Q::coef(g, p, vw3, c) * mu;
-                    if (gr) {
-                        const A qo = Q::ls(a.qprev[d], c), qn = Q::ls(a.cur[BEHF_QX + d], c);
-                        Q::ad(a.g[VW1X + d])[c] += mu * qo;
-                        Q::ad(a.g[VW2X + d])[c] += -mu * sum[d];
-                        Q::ad(a.g[vw3])[c] += -mu * dp[d];
-                        Q::ad(a.g[VU1X + d])[c] += lv * sum[d];
-                        Q::ad(a.g[VU2X + d])[c] += -lv * (qn - qo);
+                    lv[d] = lvo[d] - dl[d];
+                    const A lq = lqo[d] - dl[3 + d];
+                    mu[d] = lq - vu2[d] * lv[d];
+                    Q::ad(a.lf[BEHF_VX + d])[c] = lv[d];
+                    Q::ad(a.lf[BEHF_QX + d])[c] = vw1[d] * mu[d] + vu2[d] * lv[d];
+                    Q::ad(a.tmpV[d])[c] = vu1[d] * lv[d] - vw2[d] * mu[d];
+                    Q::ad(a.tmpV[3 + d])[c] = -vw3[d] * mu[d];
+                }
+                if (gr) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        go[VW1X + d] += mu[d] * qo[d];
+                        go[VW2X + d] += -mu[d] * sum[d];
+                        go[VU1X + d] += lv[d] * sum[d];
+                        go[VU2X + d] += -lv[d] * (qn[d] - qo[d]);
                     }
+                    go[VW3X] += -mu[0] * dp[0];
+                    const A w3z = -mu[2] * dp[2];
+                    go[VW3Y] += -mu[1] * dp[1] + (g.bug ? w3z : (A)0);
+                    go[VW3Z] += g.bug ? (A)0 : w3z;
+#pragma unroll
+                    for (int q = 0; q < 15; q++) Q::ad(a.g[q])[c] = go[q];
                 }
             } else {
-                Q::ad(a.lf[BEHF_SXX])[c] -= W::bwd(WX(0));
-                Q::ad(a.lf[BEHF_SYY])[c] -= W::bwd(WY(0));
-                Q::ad(a.lf[BEHF_SZZ])[c] -= W::bwd(WZ(0));
-                Q::ad(a.lf[BEHF_SXY])[c] -= W::fwd(WY(1)) + W::fwd(WX(1));
-                Q::ad(a.lf[BEHF_SXZ])[c] -= W::fwd(WZ(1)) + W::fwd(WX(2));
-                Q::ad(a.lf[BEHF_SYZ])[c] -= W::fwd(WZ(2)) + W::fwd(WY(2));
-                Q::ad(a.lf[BEHF_P])[c] -= W::bwd(WX(3)) + W::bwd(WY(3)) + W::bwd(WZ(3));
-                // T-slot adjoint memory of this step (its gathers ran in the KIND 0 launch)
-                const int si = slab_index(i, g.nx, g.L), sj = slab_index(j, g.ny, g.L), sk = slab_index(k, g.nz, g.L);
-                if (g.W > 0 && (si >= 0 || sj >= 0 || sk >= 0)) {
-                    A tt[7];
+                A lo[7];  // sxx syy szz sxy sxz syz p
+#pragma unroll
+                for (int q = 0; q < 7; q++) lo[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
+                // T-slot adjoint memory of this step on slab cells (its gathers ran in the KIND 0 launch)
+                const bool mem = !interior(g, i, j, k);
+                A tt[7];
+                MemUpd<A, 4, 0xC> mt;
+                if (mem) {
 #pragma unroll
                     for (int q = 0; q < 7; q++) tt[q] = Q::ad(a.tmpT[q])[c];
-                    if (si >= 0) {
-                        const long long so = slab_off(g, 0, i, j, k, si);
-                        Q::lmem(g, p, a, tt[0], 0, 4, false, i, so);
-                        Q::lmem(g, p, a, tt[3], 0, 5, false, i, so);
-                        Q::lmem(g, p, a, tt[4], 0, 6, true, i, so);
-                        Q::lmem(g, p, a, tt[5], 0, 7, true, i, so);
-                    }
-                    if (sj >= 0) {
-                        const long long so = slab_off(g, 1, i, j, k, sj);
-                        Q::lmem(g, p, a, tt[1], 1, 4, false, j, so);
-                        Q::lmem(g, p, a, tt[3], 1, 5, false, j, so);
-                        Q::lmem(g, p, a, tt[4], 1, 6, true, j, so);
-                        Q::lmem(g, p, a, tt[6], 1, 7, true, j, so);
-                    }
-                    if (sk >= 0) {
-                        const long long so = slab_off(g, 2, i, j, k, sk);
-                        Q::lmem(g, p, a, tt[2], 2, 4, false, k, so);
-                        Q::lmem(g, p, a, tt[3], 2, 5, false, k, so);
-                        Q::lmem(g, p, a, tt[5], 2, 6, true, k, so);
-                        Q::lmem(g, p, a, tt[6], 2, 7, true, k, so);
-                    }
+                    mt.load(g, p, a, i, j, k);
+                }
+                Q::ad(a.lf[BEHF_SXX])[c] = lo[0] - W::bwd(WX(0));
+                Q::ad(a.lf[BEHF_SYY])[c] = lo[1] - W::bwd(WY(0));
+                Q::ad(a.lf[BEHF_SZZ])[c] = lo[2] - W::bwd(WZ(0));
+                Q::ad(a.lf[BEHF_SXY])[c] = lo[3] - (W::fwd(WY(1)) + W::fwd(WX(1)));
+                Q::ad(a.lf[BEHF_SXZ])[c] = lo[4] - (W::fwd(WZ(1)) + W::fwd(WX(2)));
+                Q::ad(a.lf[BEHF_SYZ])[c] = lo[5] - (W::fwd(WZ(2)) + W::fwd(WY(2)));
+                Q::ad(a.lf[BEHF_P])[c] = lo[6] - (W::bwd(WX(3)) + W::bwd(WY(3)) + W::bwd(WZ(3)));
+                if (mem) {
+                    // axis x: uxx s4, wx s5, uyx s6h, uzx s7h; y: uyy, wy, uxy, uzy; z: uzz, wz, uxz, uyz
+                    const A D[3][4] = {{tt[0], tt[3], tt[4], tt[5]}, {tt[1], tt[3], tt[4], tt[6]},
+                                       {tt[2], tt[3], tt[5], tt[6]}};
+                    mt.store(a, D);
                 }
             }
 #undef WX
@@ -427,13 +542,6 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
 #undef WZ
         }
         __syncthreads();
-        if (NB == 1 && k + 1 < ke) issue(k + 1, 0);
-        if (valid) {
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-#pragma unroll
-                for (int d = 0; d < 2 * R; d++) zq[q][d] = zq[q][d + 1];
-        }
     }
 }
 
@@ -563,7 +671,7 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
     const dim3 block(32, 8, 1);
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
     const dim3 grid((nxu + 31) / 32, (nyu + 7) / 8, nzu);
-    k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a);
+    k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a, first);
     // gathers: z chunks so that about eight CTAs per SM are launched
     static int sms = 0;
     if (sms == 0) {
@@ -594,8 +702,17 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
             v.slot[ax][q] = vs[q];
             v.half[ax][q] = vh[q];
         }
-    k_gather<S, R, 0><<<ggrid, block, 0, st>>>(g, p, a, t, zc, first);
-    k_gather<S, R, 1><<<ggrid, block, 0, st>>>(g, p, a, v, zc, first);
+    const int smem = GMap<S, R>::BYTES;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_gather<S, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_gather<S, R, 0><<<ggrid, block, smem, st>>>(g, p, a, t, zc);
+    k_gather<S, R, 1><<<ggrid, block, smem, st>>>(g, p, a, v, zc);
     return cudaGetLastError();
 }
 
