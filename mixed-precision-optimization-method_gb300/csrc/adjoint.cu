@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include "behf_adjoint.cuh"
+#include "kernels_tiled.cuh"
 
 namespace behf {
 namespace {
@@ -202,52 +203,45 @@ __global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a, int
 }
 
 // Gathers, z-marching: a 32 x 8 block owns an xy tile and walks a z range.  Each gather needs 12 corrected
-// derivative-group adjoints: 4 with x stencils (staged per plane in shared memory with an x halo of R), 4 with
-// y stencils (shared memory, y halo R) and 4 with z stencils (a shared-memory ring of the 2R+2 planes k-R ..
-// k+R+1, each thread reading its own column).  Everything for plane k+1 is copied (cp.async, 16-byte chunks
-// where the tile rows are 16-byte aligned) while plane k is computed.
+// derivative-group adjoints: 4 with x stencils (x window of the plane, halo R), 4 with y stencils (y window, halo
+// R) and 4 with z stencils (a shared-memory ring of the 2R+2 planes k-R .. k+R+1, each thread reading its own
+// column).  One thread issues the TMA copies (cp.async.bulk.tensor) of plane k+1 -- its eight windows and the
+// ring's new plane k+1+R -- while plane k is computed; a full/empty mbarrier pair per stage orders them, every
+// wait is bounded.
 // "Corrected" = the adjoint CPML correction of the stencil's own axis and slot applied at the cell it was read
-// from: lD = lD~ + B (lpsi + lD~) + lprev on slab cells, lD~ elsewhere (zero off the updated cells).
+// from: lD = lD~ + B (lpsi + lD~) + lprev on slab cells, lD~ elsewhere (zero off the updated cells); applied in
+// shared memory after the copies land (x/y windows of tiles that reach a slab, ring planes inside the z slab).
 constexpr int GX = 32, GY = 8;
 
 struct StageSet {
-    const void* arr[3][4];  // [axis][k]
-    int slot[3][4];
+    int slot[3][4];  // [axis][array]: adjoint CPML memory slot and half-shift flag of each staged array
     int half[3][4];
 };
 
 template <class S, int R>
 struct G25 {
     typedef typename Traits<S>::C A;
-    template <bool CHK>
-    static __device__ __forceinline__ A corr(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const void* arr,
-                                             int ax, int slot, int half, int x, int y, int k) {
-        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) return (A)0;
-        A v = reinterpret_cast<const A*>(arr)[(long long)k * g.plane + (long long)y * g.px + x];
-        if (CHK && g.W > 0) {
-            const int pos = ax == 0 ? x : ax == 1 ? y : k;
-            const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
-            if (s >= 0) {
-                const long long so = slab_off(g, ax, x, y, k, s);
-                const A B = reinterpret_cast<const A*>(half ? p.pb2[ax] : p.pb[ax])[pos];
-                v += B * (reinterpret_cast<const A*>(a.lpsi[ax][slot])[so] + v) +
-                     reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
-            }
-        }
-        return v;
-    }
-    // the CPML correction of a value already loaded (two independent loads on slab cells)
-    static __device__ __forceinline__ A fix(const Geom& g, const DevPtrs& p, const AdjPtrs& a, A v, int ax, int slot,
-                                            int half, int x, int y, int k) {
-        if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) return v;
+    // The CPML correction v -> v + B (lpsi + v) + lprev of a value already loaded, in two phases: fix_load issues
+    // its three loads unconditionally (at slab cell 0 when (x, y, k) is outside the grid or the slab of axis ax;
+    // requires CPML), so that a caller's corrections share one memory round trip; fix_apply uses them.
+    struct Fix {
+        A B, ps, pv;
+        bool on;
+    };
+    static __device__ __forceinline__ Fix fix_load(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int ax, int slot,
+                                                   int half, int x, int y, int k) {
+        const bool in = x >= 0 && x < g.nx && y >= 0 && y < g.ny;
         const int pos = ax == 0 ? x : ax == 1 ? y : k;
         const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
-        if (s < 0) return v;
-        const long long so = slab_off(g, ax, x, y, k, s);
-        const A B = reinterpret_cast<const A*>(half ? p.pb2[ax] : p.pb[ax])[pos];
-        return v + B * (reinterpret_cast<const A*>(a.lpsi[ax][slot])[so] + v) +
-               reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
+        Fix f;
+        f.on = in && s >= 0;
+        const long long so = f.on ? slab_off(g, ax, x, y, k, s) : 0;
+        f.B = reinterpret_cast<const A*>(half ? p.pb2[ax] : p.pb[ax])[f.on ? pos : 0];
+        f.ps = reinterpret_cast<const A*>(a.lpsi[ax][slot])[so];
+        f.pv = reinterpret_cast<const A*>(a.lprv[ax][slot])[so];
+        return f;
     }
+    static __device__ __forceinline__ A fix_apply(const Fix& f, A v) { return f.on ? v + f.B * (f.ps + v) + f.pv : v; }
     // w[d + R] = L[c + d]:  fwdL = sum_m w_m (L[+m] - L[1-m]),  bwdL = sum_m w_m (L[m-1] - L[-m])
     template <class F>
     static __device__ __forceinline__ A fwd(F w) {
@@ -265,187 +259,226 @@ struct G25 {
     }
 };
 
-// Asynchronous global -> shared copies (cp.async, no registers held): the first `bytes` bytes come from src,
-// the rest of the BYTES is zero-filled (bytes = 0 reads nothing).
-__device__ __forceinline__ uint32_t sh_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void* dst, const void* src, int bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sh_u32(dst)), "l"(src), "n"(BYTES), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// Dynamic shared memory of a gather CTA (elements of A): two plane buffers of the x windows [4][GY][XWP] and
-// of the y windows [4][YH][GX], then the z ring [4][ZS][GY * GX].  Rows of the x window start at the 16-byte
-// aligned column i0 - R = 32 bx and are padded to whole 16-byte chunks; y-window and z-ring rows start at
-// i0 = R + 32 bx, 16-byte aligned when R * sizeof(A) is (YV), else copied element by element.
-template <class S, int R>
+// Shared memory of a gather CTA: NS = 2 stages of [4 x windows][4 y windows] (adjoint arrays, type A), then the
+// z ring [4][ZS] of row boxes.  x windows start at the 16-byte aligned column i0 - R = 32 bx, padded to whole
+// 16-byte chunks (XWP); y windows and ring rows start at i0 = R + 32 bx when that is 16-byte aligned (YV), else at
+// i0 - R with the x window's width (YC = column of i0 in them).  With SNAP (the T^T gather of the 16-bit kinds)
+// each stage also holds [4 x][4 y] windows of the forward snapshot (type S: sxx sxy sxz p / syy sxy syz p) and a
+// second ring holds its z rows (szz sxz syz p), for the stencils of the V-coefficient gradients.  Every box starts
+// on a 128-byte boundary.
+template <class S, int R, int KIND>
 struct GMap {
     typedef typename Traits<S>::C A;
-    static constexpr int CH = 16 / (int)sizeof(A);
     static constexpr int XW = GX + 2 * R;
-    static constexpr int XWP = (XW + CH - 1) / CH * CH;
     static constexpr int YH = GY + 2 * R;
-    static constexpr int ZS = 2 * R + 2;
+    static constexpr int CH = 16 / (int)sizeof(A);
+    static constexpr int XWP = (XW + CH - 1) / CH * CH;
     static constexpr bool YV = (R * (int)sizeof(A)) % 16 == 0;
-    static constexpr int XB = 4 * GY * XWP, YB = 4 * YH * GX;
-    static constexpr int X_OFF = 0, Y_OFF = 2 * XB, Z_OFF = Y_OFF + 2 * YB;
-    static constexpr int BYTES = (Z_OFF + 4 * ZS * GY * GX) * (int)sizeof(A);
+    static constexpr int YW = YV ? GX : XWP;
+    static constexpr int YC = YV ? 0 : R;
+    static constexpr bool SNAP = KIND == 0 && sizeof(S) == 2;
+    static constexpr int CHS = 16 / (int)sizeof(S);
+    static constexpr int XWPS = (XW + CHS - 1) / CHS * CHS;
+    static constexpr bool YVS = (R * (int)sizeof(S)) % 16 == 0;
+    static constexpr int YWS = YVS ? GX : XWPS;
+    static constexpr int YCS = YVS ? 0 : R;
+    static constexpr int ZS = 2 * R + 2;
+    static constexpr int NS = 2;
+    static constexpr int XBOX = tiled::al128(XWP * GY * (int)sizeof(A));
+    static constexpr int YBOX = tiled::al128(YW * YH * (int)sizeof(A));
+    static constexpr int ZBOX = tiled::al128(YW * GY * (int)sizeof(A));
+    static constexpr int XBOXS = SNAP ? tiled::al128(XWPS * GY * (int)sizeof(S)) : 0;
+    static constexpr int YBOXS = SNAP ? tiled::al128(YWS * YH * (int)sizeof(S)) : 0;
+    static constexpr int ZBOXS = SNAP ? tiled::al128(YWS * GY * (int)sizeof(S)) : 0;
+    static constexpr int SOFF = 4 * XBOX + 4 * YBOX;  // snapshot windows within a stage
+    static constexpr int STAGE = SOFF + 4 * XBOXS + 4 * YBOXS;
+    static constexpr int RING = NS * STAGE;
+    static constexpr int RINGS = RING + 4 * ZS * ZBOX;
+    static constexpr int BYTES = RINGS + 4 * ZS * ZBOXS;
+    static constexpr uint32_t STAGE_TX = 4u * (XWP * GY + YW * YH) * (uint32_t)sizeof(A);
+    static constexpr uint32_t Z_TX = 4u * YW * GY * (uint32_t)sizeof(A);
+    static constexpr uint32_t STAGE_TXS = SNAP ? 4u * (XWPS * GY + YWS * YH) * (uint32_t)sizeof(S) : 0u;
+    static constexpr uint32_t Z_TXS = SNAP ? 4u * YWS * GY * (uint32_t)sizeof(S) : 0u;
 };
 
 // KIND 0: T^T gather (X: T0 s4, T4 s6h, T5 s7h, T3 s5;  Y: T1 s4, T4 s6h, T6 s7h, T3 s5;
 //                      Z: T2 s4, T5 s6h, T6 s7h, T3 s5), then V^T per cell.
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
 //                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update.
+// maps.m[0..3]: x windows, [4..7]: y windows, [8..11]: ring rows, in the order above; smaps: the same for the
+// snapshot arrays of this step (SNAP only).
 template <class S, int R, int KIND>
-__global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a, StageSet ss, int zc) {
+__global__ void __launch_bounds__(256, 2)
+    k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
+             AdjPtrs a, StageSet ss, int zc) {
     typedef G25<S, R> W;
     typedef Adj<S, R> Q;
-    typedef GMap<S, R> M;
+    typedef GMap<S, R, KIND> M;
     typedef typename W::A A;
-    extern __shared__ __align__(16) unsigned char gsm_raw[];
-    A* const gsm = reinterpret_cast<A*>(gsm_raw);
-    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * GX + tx;
+    using namespace tiled;
+    extern __shared__ __align__(128) unsigned char gsm_raw[];
+    __shared__ __align__(8) uint64_t bfull[M::NS], bempty[M::NS];
+    unsigned char* sm = gsm_raw + ((128u - (smem_u32(gsm_raw) & 127u)) & 127u);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * GX + tx;
     const int i0 = R + blockIdx.x * GX, j0 = R + blockIdx.y * GY;
     const int i = i0 + tx, j = j0 + ty;
     const bool valid = i < g.nx - R && j < g.ny - R;
     const int kb = R + blockIdx.z * zc, ke = min(kb + zc, g.nz - R);
     if (kb >= ke) return;
     const long long sy = g.px, sz = g.plane;
-    static_assert(M::YH <= 16 && M::XWP <= 64, "window larger than the block's copy pattern");
-    auto shx = [&](int bf, int q, int r, int col) -> A& { return gsm[M::X_OFF + bf * M::XB + (q * GY + r) * M::XWP + col]; };
-    auto shy = [&](int bf, int q, int r, int col) -> A& { return gsm[M::Y_OFF + bf * M::YB + (q * M::YH + r) * GX + col]; };
-    auto zr = [&](int q, int slot) -> A* { return gsm + M::Z_OFF + (q * M::ZS + slot) * (GY * GX); };
+    auto X = [&](int st, int q) { return reinterpret_cast<A*>(sm + st * M::STAGE + q * M::XBOX); };
+    auto Y = [&](int st, int q) { return reinterpret_cast<A*>(sm + st * M::STAGE + 4 * M::XBOX + q * M::YBOX); };
+    auto Z = [&](int q, int slot) { return reinterpret_cast<A*>(sm + M::RING + (q * M::ZS + slot) * M::ZBOX); };
+    auto XS = [&](int st, int q) { return reinterpret_cast<S*>(sm + st * M::STAGE + M::SOFF + q * M::XBOXS); };
+    auto YS = [&](int st, int q) {
+        return reinterpret_cast<S*>(sm + st * M::STAGE + M::SOFF + 4 * M::XBOXS + q * M::YBOXS);
+    };
+    auto ZS_ = [&](int q, int slot) { return reinterpret_cast<S*>(sm + M::RINGS + (q * M::ZS + slot) * M::ZBOXS); };
+    const int yx0 = M::YV ? i0 : i0 - R;     // first column of the y windows and ring rows
+    const int yx0s = M::YVS ? i0 : i0 - R;   // the same for the snapshot
+    // the snapshot is staged only where the tile and z range hold cells outside every CPML slab
+    auto has_int = [&](int lo, int hi, int n) { return g.W == 0 || max(lo, g.L) <= min(hi, n - 2 - g.L); };
+    const bool snap = M::SNAP && a.grad && has_int(i0, i0 + GX - 1, g.nx) && has_int(j0, j0 + GY - 1, g.ny) &&
+                      has_int(kb, ke - 1, g.nz);
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
-    // bytes of the 16-byte chunk at column x that lie inside the grid (rows outside it: 0)
-    auto chunk_bytes = [&](int x, int y) {
-        const int n = (g.nx - x) * (int)sizeof(A);
-        return (y >= g.ny || n <= 0) ? 0 : (n < 16 ? n : 16);
+    const bool fixcta = cx || cy;
+
+    if (tid == 0) {
+        for (int s = 0; s < M::NS; s++) {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], GY);  // one arrival per warp
+        }
+        fence_init();
+    }
+    __syncthreads();
+
+    // stage st <- plane kk: the eight windows and the ring plane kk + R (warm-up: kk - R .. kk + R)
+    auto issue = [&](int st, int kk, bool warm) {
+        uint64_t* br = &bfull[st];
+        const uint32_t nz_ = warm ? 2 * R + 1 : 1;
+        mbar_expect_tx(br, M::STAGE_TX + M::Z_TX * nz_ + (snap ? M::STAGE_TXS + M::Z_TXS * nz_ : 0u));
+#pragma unroll
+        for (int q = 0; q < 4; q++) tma3(X(st, q), &maps.m[q], br, i0 - R, j0, kk);
+#pragma unroll
+        for (int q = 0; q < 4; q++) tma3(Y(st, q), &maps.m[4 + q], br, yx0, j0 - R, kk);
+        for (int z = warm ? kk - R : kk + R; z <= kk + R; z++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) tma3(Z(q, z % M::ZS), &maps.m[8 + q], br, yx0, j0, z);
+        if (snap) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) tma3(XS(st, q), &smaps.m[q], br, i0 - R, j0, kk);
+#pragma unroll
+            for (int q = 0; q < 4; q++) tma3(YS(st, q), &smaps.m[4 + q], br, yx0s, j0 - R, kk);
+            for (int z = warm ? kk - R : kk + R; z <= kk + R; z++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) tma3(ZS_(q, z % M::ZS), &smaps.m[8 + q], br, yx0s, j0, z);
+        }
     };
-    // z ring: plane zz of the four z-stencil arrays into its slot (CPML-corrected element by element on a z-slab plane)
-    auto zfill = [&](int zz) {
-        const int slot = zz % M::ZS;
-        const bool zslab = g.W > 0 && slab_index(zz, g.nz, g.L) >= 0;
-        if (zslab || !M::YV) {
-            if (valid) {
+    uint32_t fph = 0, eph = 0;
+    uint32_t pend = 0;  // thread 0, bit s: stage s issued and not yet consumed (for the drain after a timeout)
+    if (tid == 0) {
+        issue(0, kb, true);
+        pend = 1u;
+    }
+    bool failed = false;
+    for (int k = kb, it = 0; k < ke; k++, it++) {
+        const int st = it & 1;
+        bool ok = true;
+        if (tid == 0 && k + 1 < ke) {
+            const int sn = st ^ 1;
+            if (it >= 1) {  // stage sn was read in iteration it - 1: wait until every warp released it
+                ok = mbar_wait(&bempty[sn], (eph >> sn) & 1u);
+                eph ^= 1u << sn;
+            }
+            if (ok) {
+                fence_async();
+                issue(sn, k + 1, false);
+                pend |= 1u << sn;
+            }
+        }
+        if (ok) ok = mbar_wait(&bfull[st], (fph >> st) & 1u);
+        // timeout: every thread leaves together (the x/y corrections below hold block barriers)
+        if (fixcta ? !__syncthreads_and(ok) : !__all_sync(0xffffffffu, ok)) {
+            failed = true;
+            break;
+        }
+        fph ^= 1u << st;
+        if (tid == 0) pend &= ~(1u << st);
+        // ring planes that arrived with this stage and lie in the z slab: each thread corrects its own column
+        if (g.W > 0 && valid) {
+            for (int z = it == 0 ? k - R : k + R; z <= k + R; z++) {
+                if (slab_index(z, g.nz, g.L) < 0) continue;
+                typename W::Fix f[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) f[q] = W::fix_load(g, p, a, 2, ss.slot[2][q], ss.half[2][q], i, j, z);
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    if (zslab) {
-                        zr(q, slot)[t] = W::template corr<true>(g, p, a, ss.arr[2][q], 2, ss.slot[2][q], ss.half[2][q],
-                                                                i, j, zz);
-                    } else {
-                        cp_async<sizeof(A)>(zr(q, slot) + t,
-                                            reinterpret_cast<const A*>(ss.arr[2][q]) + zz * sz + j * sy + i,
-                                            (int)sizeof(A));
-                    }
+                    A* e = Z(q, z % M::ZS) + ty * M::YW + M::YC + tx;
+                    *e = W::fix_apply(f[q], *e);
                 }
             }
-        } else {
-            // warp ty copies row ty: (array, chunk) pairs over the lanes
-            constexpr int NCH = GX / M::CH;
-            for (int u = tx; u < 4 * NCH; u += 32) {
-                const int q = u / NCH, ch = u % NCH;
-                const int x = i0 + ch * M::CH, y = j;
-                const int nb = chunk_bytes(x, y);
-                const long long off = nb ? zz * sz + (long long)y * sy + x : 0;
-                cp_async<16>(zr(q, slot) + ty * GX + ch * M::CH, reinterpret_cast<const A*>(ss.arr[2][q]) + off, nb);
-            }
         }
-    };
-    // x and y windows of plane kk into buffer bf (zero outside the grid)
-    auto issue = [&](int kk, int bf) {
-        const long long pk = (long long)kk * sz;
-        {  // x window: warp ty copies row ty, 16-byte chunks
-            constexpr int NCH = M::XWP / M::CH;
-            const int y = j0 + ty;
-            for (int u = tx; u < 4 * NCH; u += 32) {
-                const int q = u / NCH, ch = u % NCH;
-                const int x = i0 - R + ch * M::CH;
-                const int nb = chunk_bytes(x, y);
-                const long long off = nb ? pk + (long long)y * sy + x : 0;
-                cp_async<16>(&shx(bf, q, ty, ch * M::CH), reinterpret_cast<const A*>(ss.arr[0][q]) + off, nb);
-            }
-        }
-        if (M::YV) {  // y window: the YH rows x 4 arrays x (GX / CH) chunks over the block
-            constexpr int NCH = GX / M::CH;
-            for (int u = t; u < M::YH * 4 * NCH; u += GX * GY) {
-                const int ch = u % NCH, rq = u / NCH, q = rq % 4, r = rq / 4;
-                const int x = i0 + ch * M::CH, y = j0 - R + r;
-                const int nb = chunk_bytes(x, y);
-                const long long off = nb ? pk + (long long)y * sy + x : 0;
-                cp_async<16>(&shy(bf, q, r, ch * M::CH), reinterpret_cast<const A*>(ss.arr[1][q]) + off, nb);
-            }
-        } else {
+        if (fixcta) {  // CPML corrections of the x/y windows near a slab: each thread rewrites its own elements
+            if (cx) {  // x window: row ty, columns tx and tx + 32 < XW
+                typename W::Fix f[2][4];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int r = ty + 8 * h;
-                if (r < M::YH) {
-                    const int x = i0 + tx, y = j0 - R + r;
-                    const bool in = x < g.nx && y < g.ny;
-                    const long long off = in ? pk + (long long)y * sy + x : 0;
+                for (int h = 0; h < 2; h++)
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        cp_async<sizeof(A)>(&shy(bf, q, r, tx), reinterpret_cast<const A*>(ss.arr[1][q]) + off,
-                                            in ? (int)sizeof(A) : 0);
+                        f[h][q] = W::fix_load(g, p, a, 0, ss.slot[0][q], ss.half[0][q], i0 - R + tx + 32 * h, j0 + ty, k);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int cc = tx + 32 * h;
+                    if (cc < M::XW)
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            A* e = X(st, q) + ty * M::XWP + cc;
+                            *e = W::fix_apply(f[h][q], *e);
+                        }
                 }
             }
-        }
-    };
-    for (int zz = kb - R; zz <= kb + R; zz++) zfill(zz);
-    issue(kb, 0);
-    cp_async_commit();
-    for (int k = kb; k < ke; k++) {
-        const int bf = (k - kb) & 1;
-        if (k + 1 < ke) {
-            // the other window buffer and the ring slot of plane k - R - 1 were released by the barrier that ended
-            // plane k - 1
-            issue(k + 1, bf ^ 1);
-            zfill(k + 1 + R);
-            cp_async_commit();
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-        if (cx || cy) {  // CPML corrections of the copied windows near a slab (all loads, then the writes)
-            A fxv[2][4], fyv[2][4];
+            if (cy) {  // y window: rows ty and ty + 8 < YH, column tx
+                typename W::Fix f[2][4];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int cc = tx + 32 * h, r = ty + 8 * h;
+                for (int h = 0; h < 2; h++)
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (cx && cc < M::XW)
-                        fxv[h][q] = W::fix(g, p, a, shx(bf, q, ty, cc), 0, ss.slot[0][q], ss.half[0][q], i0 - R + cc,
-                                           j0 + ty, k);
-                    if (cy && r < M::YH)
-                        fyv[h][q] = W::fix(g, p, a, shy(bf, q, r, tx), 1, ss.slot[1][q], ss.half[1][q], i0 + tx,
-                                           j0 - R + r, k);
-                }
-            }
-            __syncthreads();  // every thread has read the raw windows
+                    for (int q = 0; q < 4; q++)
+                        f[h][q] = W::fix_load(g, p, a, 1, ss.slot[1][q], ss.half[1][q], i0 + tx, j0 - R + ty + 8 * h, k);
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int cc = tx + 32 * h, r = ty + 8 * h;
+                for (int h = 0; h < 2; h++) {
+                    const int r = ty + 8 * h;
+                    if (r < M::YH)
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (cx && cc < M::XW) shx(bf, q, ty, cc) = fxv[h][q];
-                    if (cy && r < M::YH) shy(bf, q, r, tx) = fyv[h][q];
+                        for (int q = 0; q < 4; q++) {
+                            A* e = Y(st, q) + r * M::YW + M::YC + tx;
+                            *e = W::fix_apply(f[h][q], *e);
+                        }
                 }
             }
             __syncthreads();
         }
         if (valid) {
             const long long c = k * sz + j * sy + i;
-            int zs[2 * R + 1];  // ring slots of planes k-R .. k+R
+            // element offsets: array q of the x (y) windows at q * XE (q * YE) from the first, ring row of array q
+            // and plane k + d at q * ZS * ZE + zoff[d + R]
+            constexpr int XE = M::XBOX / (int)sizeof(A), YE = M::YBOX / (int)sizeof(A), ZE = M::ZBOX / (int)sizeof(A);
+            const A* xb = X(st, 0) + ty * M::XWP + tx + R;
+            const A* yb = Y(st, 0) + (ty + R) * M::YW + M::YC + tx;
+            const A* zb = Z(0, 0) + ty * M::YW + M::YC + tx;
+            int zoff[2 * R + 1];
+            {
+                int s0 = (k - R) % M::ZS;
 #pragma unroll
-            for (int d = 0; d <= 2 * R; d++) zs[d] = (k - R + d) % M::ZS;
-#define WX(q) [&](int d) { return shx(bf, q, ty, tx + R + d); }
-#define WY(q) [&](int d) { return shy(bf, q, ty + R + d, tx); }
-#define WZ(q) [&](int d) { return zr(q, zs[R + d])[t]; }
+                for (int d = 0; d <= 2 * R; d++) {
+                    zoff[d] = s0 * ZE;
+                    s0 = s0 + 1 == M::ZS ? 0 : s0 + 1;
+                }
+            }
+#define WX(q) [&](int d) { return xb[(q) * XE + d]; }
+#define WY(q) [&](int d) { return yb[(q) * YE + d * M::YW]; }
+#define WZ(q) [&](int d) { return zb[(q) * M::ZS * ZE + zoff[R + d]]; }
             // Each cell issues all its global loads before its first global store (see k_adj_a).
             if (KIND == 0) {
                 // V^T at this cell with lv = lv_old - dl[0..2], lq' = lq_old - dl[3..5]
@@ -463,12 +496,38 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
                 const bool gr = a.grad && interior(g, i, j, k);
                 A sum[3], dp[3], qo[3], qn[3], go[15];
                 if (gr) {
-                    sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) + Q::bwd(a.cur[BEHF_SXZ], c, sz);
-                    sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sz);
-                    sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) + Q::bwd(a.cur[BEHF_SYZ], c, sy);
-                    dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
-                    dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
-                    dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
+                    if constexpr (M::SNAP) {  // snapshot stencils from the staged windows (gr implies snap)
+                        constexpr int XES = M::XBOXS / (int)sizeof(S), YES = M::YBOXS / (int)sizeof(S);
+                        constexpr int ZES = M::ZBOXS / (int)sizeof(S);
+                        const S* xs = XS(st, 0) + ty * M::XWPS + tx + R;
+                        const S* ys = YS(st, 0) + (ty + R) * M::YWS + M::YCS + tx;
+                        const S* zsb = ZS_(0, 0) + ty * M::YWS + M::YCS + tx;
+                        const int zs0 = (k - R) % M::ZS;
+                        auto zsl = [&](int d) { return zs0 + R + d >= M::ZS ? zs0 + R + d - M::ZS : zs0 + R + d; };
+#define SXW(q) [&](int d) { return Q::ls(xs, (q) * XES + d); }
+#define SYW(q) [&](int d) { return Q::ls(ys, (q) * YES + d * M::YWS); }
+#define SZW(q) [&](int d) { return Q::ls(zsb, ((q) * M::ZS + zsl(d)) * ZES); }
+                        // x: sxx sxy sxz p;  y: syy sxy syz p;  z: szz sxz syz p
+                        sum[0] = W::fwd(SXW(0)) + W::bwd(SYW(1)) + W::bwd(SZW(1));
+                        sum[1] = W::fwd(SYW(0)) + W::bwd(SXW(1)) + W::bwd(SZW(2));
+                        sum[2] = W::fwd(SZW(0)) + W::bwd(SXW(2)) + W::bwd(SYW(2));
+                        dp[0] = W::fwd(SXW(3));
+                        dp[1] = W::fwd(SYW(3));
+                        dp[2] = W::fwd(SZW(3));
+#undef SXW
+#undef SYW
+#undef SZW
+                    } else {
+                        sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) +
+                                 Q::bwd(a.cur[BEHF_SXZ], c, sz);
+                        sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) +
+                                 Q::bwd(a.cur[BEHF_SYZ], c, sz);
+                        sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) +
+                                 Q::bwd(a.cur[BEHF_SYZ], c, sy);
+                        dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
+                        dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
+                        dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
+                    }
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         qo[d] = Q::ls(a.qprev[d], c);
@@ -541,8 +600,18 @@ __global__ void __launch_bounds__(256, 2) k_gather(Geom g, DevPtrs p, AdjPtrs a,
 #undef WY
 #undef WZ
         }
-        __syncthreads();
+        // generic-proxy writes to shared memory (the corrections) before the TMA that will overwrite it
+        if (g.W > 0) fence_async();
+        __syncwarp();
+        if (tx == 0) mbar_arrive(&bempty[st]);
     }
+    if (failed) atomicExch(g.err, 1);
+    if (tid == 0)  // drain the copies still in flight before the CTA's shared memory is released
+        for (int s = 0; s < M::NS; s++)
+            if ((pend >> s) & 1u) {
+                mbar_wait(&bfull[s], (fph >> s) & 1u);
+                fph ^= 1u << s;
+            }
 }
 
 #undef CELL_INDEX
@@ -667,7 +736,8 @@ __global__ void k_grad_moduli(GradModArgs a) {
 }
 
 template <class S, int R>
-cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st) {
+cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap, int first,
+                  cudaStream_t st) {
     const dim3 block(32, 8, 1);
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
     const dim3 grid((nxu + 31) / 32, (nyu + 7) / 8, nzu);
@@ -678,7 +748,7 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 132;
+        if (sms <= 0) sms = 148;
     }
     const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
     int nch = (8 * sms + nxy - 1) / nxy;
@@ -687,44 +757,105 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, 
     const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);
     StageSet t{}, v{};
     // T^T gather: x {T0 s4, T4 s6h, T5 s7h, T3 s5}, y {T1 s4, T4 s6h, T6 s7h, T3 s5}, z {T2 s4, T5 s6h, T6 s7h, T3 s5}
-    const int tq[3][4] = {{0, 4, 5, 3}, {1, 4, 6, 3}, {2, 5, 6, 3}};
     const int ts[4] = {4, 6, 7, 5}, th[4] = {0, 1, 1, 0};
-    const int tz_s[4] = {4, 6, 7, 5};
     // V^T gather: x {V0 s0h, V1 s2, V2 s3, V3 s1h}, y {V1 s0h, V0 s2, V2 s3, V4 s1h}, z {V2 s0h, V0 s2, V1 s3, V5 s1h}
-    const int vq[3][4] = {{0, 1, 2, 3}, {1, 0, 2, 4}, {2, 0, 1, 5}};
     const int vs[4] = {0, 2, 3, 1}, vh[4] = {1, 0, 0, 1};
     for (int ax = 0; ax < 3; ax++)
         for (int q = 0; q < 4; q++) {
-            t.arr[ax][q] = a.tmpT[tq[ax][q]];
-            t.slot[ax][q] = ax == 2 ? tz_s[q] : ts[q];
+            t.slot[ax][q] = ts[q];
             t.half[ax][q] = th[q];
-            v.arr[ax][q] = a.tmpV[vq[ax][q]];
             v.slot[ax][q] = vs[q];
             v.half[ax][q] = vh[q];
         }
-    const int smem = GMap<S, R>::BYTES;
+    const int smem0 = GMap<S, R, 0>::BYTES + 128, smem1 = GMap<S, R, 1>::BYTES + 128;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem0);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_gather<S, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            e = cudaFuncSetAttribute(k_gather<S, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_gather<S, R, 0><<<ggrid, block, smem, st>>>(g, p, a, t, zc);
-    k_gather<S, R, 1><<<ggrid, block, smem, st>>>(g, p, a, v, zc);
+    if (GMap<S, R, 0>::SNAP && a.grad && !snap) return cudaErrorInvalidValue;
+    k_gather<S, R, 0><<<ggrid, block, smem0, st>>>(m.t, snap ? *snap : m.t, g, p, a, t, zc);
+    k_gather<S, R, 1><<<ggrid, block, smem1, st>>>(m.v, m.v, g, p, a, v, zc);
     return cudaGetLastError();
+}
+
+// Boxes of one gather's maps over arrays of T: x windows XWP x GY, y windows YW x YH, ring rows YW x GY.
+template <class T, int XWP, int YW, int YH>
+bool build_gather_maps(const Geom& g, void* const x[4], void* const y[4], void* const z[4], GatherMaps* gm) {
+    bool ok = true;
+    for (int q = 0; q < 4; q++) {
+        ok = ok && tiled::encode<T>(&gm->m[q], g, x[q], XWP, GY);
+        ok = ok && tiled::encode<T>(&gm->m[4 + q], g, y[q], YW, YH);
+        ok = ok && tiled::encode<T>(&gm->m[8 + q], g, z[q], YW, GY);
+    }
+    return ok;
+}
+
+template <class S, int R>
+cudaError_t build_maps_r(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
+    // same array order as the StageSet tables in adj_r
+    void* const tx_[4] = {a.tmpT[0], a.tmpT[4], a.tmpT[5], a.tmpT[3]};
+    void* const ty_[4] = {a.tmpT[1], a.tmpT[4], a.tmpT[6], a.tmpT[3]};
+    void* const tz_[4] = {a.tmpT[2], a.tmpT[5], a.tmpT[6], a.tmpT[3]};
+    void* const vx_[4] = {a.tmpV[0], a.tmpV[1], a.tmpV[2], a.tmpV[3]};
+    void* const vy_[4] = {a.tmpV[1], a.tmpV[0], a.tmpV[2], a.tmpV[4]};
+    void* const vz_[4] = {a.tmpV[2], a.tmpV[0], a.tmpV[1], a.tmpV[5]};
+    if (!tiled::encoder()) return cudaErrorNotSupported;
+    typedef GMap<S, R, 0> M;
+    typedef typename M::A A;
+    const bool ok = build_gather_maps<A, M::XWP, M::YW, M::YH>(g, tx_, ty_, tz_, &m->t) &&
+                    build_gather_maps<A, M::XWP, M::YW, M::YH>(g, vx_, vy_, vz_, &m->v);
+    return ok ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <class S, int R>
+cudaError_t build_snap_maps_r(const Geom& g, void* const f[kNField], GatherMaps* m) {
+    typedef GMap<S, R, 0> M;
+    if (!M::SNAP) return cudaSuccess;
+    if (!tiled::encoder()) return cudaErrorNotSupported;
+    void* const x[4] = {f[BEHF_SXX], f[BEHF_SXY], f[BEHF_SXZ], f[BEHF_P]};
+    void* const y[4] = {f[BEHF_SYY], f[BEHF_SXY], f[BEHF_SYZ], f[BEHF_P]};
+    void* const z[4] = {f[BEHF_SZZ], f[BEHF_SXZ], f[BEHF_SYZ], f[BEHF_P]};
+    return build_gather_maps<S, M::XWPS, M::YWS, M::YH>(g, x, y, z, m) ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace
 
 template <class S>
-cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st) {
+cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
     switch (g.R) {
-        case 1: return adj_r<S, 1>(g, p, a, first, st);
-        case 2: return adj_r<S, 2>(g, p, a, first, st);
-        case 3: return adj_r<S, 3>(g, p, a, first, st);
-        case 4: return adj_r<S, 4>(g, p, a, first, st);
+        case 1: return build_maps_r<S, 1>(g, a, m);
+        case 2: return build_maps_r<S, 2>(g, a, m);
+        case 3: return build_maps_r<S, 3>(g, a, m);
+        case 4: return build_maps_r<S, 4>(g, a, m);
+    }
+    return cudaErrorInvalidValue;
+}
+template <class S>
+bool adj_snap_staged() {
+    return sizeof(S) == 2;
+}
+template <class S>
+cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* m) {
+    switch (g.R) {
+        case 1: return build_snap_maps_r<S, 1>(g, f, m);
+        case 2: return build_snap_maps_r<S, 2>(g, f, m);
+        case 3: return build_snap_maps_r<S, 3>(g, f, m);
+        case 4: return build_snap_maps_r<S, 4>(g, f, m);
+    }
+    return cudaErrorInvalidValue;
+}
+template <class S>
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap,
+                     int first, cudaStream_t st) {
+    switch (g.R) {
+        case 1: return adj_r<S, 1>(g, p, a, m, snap, first, st);
+        case 2: return adj_r<S, 2>(g, p, a, m, snap, first, st);
+        case 3: return adj_r<S, 3>(g, p, a, m, snap, first, st);
+        case 4: return adj_r<S, 4>(g, p, a, m, snap, first, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -751,7 +882,11 @@ cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st) {
 }
 
 #define BEHF_ADJ_INST(S)                                                                                         \
-    template cudaError_t adj_step<S>(const Geom&, const DevPtrs&, const AdjPtrs&, int, cudaStream_t);          \
+    template cudaError_t adj_build_maps<S>(const Geom&, const AdjPtrs&, AdjMaps*);                             \
+    template bool adj_snap_staged<S>();                                                                        \
+    template cudaError_t adj_build_snap_maps<S>(const Geom&, void* const*, GatherMaps*);                       \
+    template cudaError_t adj_step<S>(const Geom&, const DevPtrs&, const AdjPtrs&, const AdjMaps&,              \
+                                     const GatherMaps*, int, cudaStream_t);                                    \
     template cudaError_t adj_record<S>(const AdjPtrs&, const long long*, const int*, int, const double*, int, int, \
                                        const AdjScales&, cudaStream_t);                                          \
     template cudaError_t adj_point<S>(const AdjPtrs&, long long, int, double, const float*, int, int, double*,  \

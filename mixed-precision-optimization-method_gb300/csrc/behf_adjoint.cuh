@@ -12,6 +12,8 @@
 //   per slab cell: the adjoint CPML memory update  L = lpsi + lD;  lpsi = A L;  lprev = A B L;
 // fused into three launches per step (adjoint.cu).
 #pragma once
+#include <cuda.h>
+
 #include "behf_internal.cuh"
 
 namespace behf {
@@ -28,13 +30,34 @@ struct AdjPtrs {
     int grad;                // accumulate coefficient gradients
 };
 
+// Tensor maps of the twelve staged arrays of one gather (x windows, y windows, z-ring rows; adjoint.cu), and of
+// both gathers of a gradient run (built once: the scratch arrays do not move).
+struct alignas(64) GatherMaps {
+    CUtensorMap m[12];
+};
+struct alignas(64) AdjMaps {
+    GatherMaps t, v;  // T^T gather (tmpT), V^T gather (tmpV)
+};
+
 struct AdjScales {
     double s[kNField];       // multiplier of the adjoint source per recorded field (alpha / storage scale)
 };
 
-// T^T and V^T of one step (three launches); first = 1 on the first backward step (no V-slot memory pending).
+// Encode the gathers' tensor maps for the scratch arrays of `a` (host; cudaErrorNotSupported without the driver's
+// tensor-map encoder).
 template <class S>
-cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int first, cudaStream_t st);
+cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m);
+// The T^T gather of the 16-bit kinds stages the forward snapshot of the step (its stress and pressure stencils
+// for the V-coefficient gradients) through tensor maps built per snapshot buffer by adj_build_snap_maps.
+template <class S>
+bool adj_snap_staged();
+template <class S>
+cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* m);
+// T^T and V^T of one step (three launches); first = 1 on the first backward step (no V-slot memory pending);
+// snap: the maps of a.cur (required when adj_snap_staged<S>() and a.grad, else ignored).
+template <class S>
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap,
+                     int first, cudaStream_t st);
 // record^T: lf[comp[r]][off[r]] += adj[r * nt + it] * sc.s[comp[r]]  (atomic: receivers may share a cell)
 template <class S>
 cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, int nrec, const double* adj, int nt,

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -1049,6 +1050,20 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemsetAsync(d_gw, 0, (size_t)nt * 8, c->stream));
     CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
     a.grad = 1;
+    AdjMaps* maps = static_cast<AdjMaps*>(std::aligned_alloc(alignof(AdjMaps), sizeof(AdjMaps)));
+    if (!maps) return fail(BEHF_ERR_ALLOC, "host allocation of the adjoint tensor maps");
+    std::unique_ptr<AdjMaps, void (*)(void*)> maps_owner(maps, std::free);
+    CK(adj_build_maps<S>(g, a, maps));
+    // tensor maps of every snapshot buffer (slot u holds the fields after V of step s0 + u - 1)
+    std::vector<GatherMaps> snap_maps;
+    if (adj_snap_staged<S>()) {
+        snap_maps.resize(S_ + 1);
+        for (int u = 0; u <= S_; u++) {
+            void* f[kNField];
+            for (int q = 0; q < kNField; q++) f[q] = snap + snap_bytes * u + (size_t)q * align256(nf * c->es);
+            CK(adj_build_snap_maps<S>(g, f, &snap_maps[u]));
+        }
+    }
 
     auto copy_state = [&](char* dst, bool save) -> cudaError_t {
         char* q = dst;
@@ -1140,7 +1155,8 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(it - s0 + 1, f);
             for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(it - s0, BEHF_QX + d);
             CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
-            CK(adj_step<S>(g, c->p, a, it == nt - 1 ? 1 : 0, c->stream));
+            CK(adj_step<S>(g, c->p, a, *maps, snap_maps.empty() ? nullptr : &snap_maps[it - s0 + 1],
+                           it == nt - 1 ? 1 : 0, c->stream));
             CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
             c->launches += 5;
         }

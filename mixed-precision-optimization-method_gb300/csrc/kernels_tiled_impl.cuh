@@ -1,10 +1,6 @@
 // kernels_tiled_impl.cuh -- bodies of the z-marching kernels (included once per storage precision by
 // kernels_tiled_{f16,bf16,f32}.cu so the three instantiations compile in parallel).
 #pragma once
-#include <cudaTypedefs.h>
-
-#include <mutex>
-
 #include "kernels_tiled.cuh"
 
 namespace behf {
@@ -570,39 +566,6 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
 }
 
 // ----------------------------------------------------------------------------------------- host side
-inline PFN_cuTensorMapEncodeTiled_v12000 encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    });
-    return fn;
-}
-
-template <class T> inline CUtensorMapDataType dtype_of();
-template <> inline CUtensorMapDataType dtype_of<__half>() { return CU_TENSOR_MAP_DATA_TYPE_FLOAT16; }
-template <> inline CUtensorMapDataType dtype_of<__nv_bfloat16>() { return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16; }
-template <> inline CUtensorMapDataType dtype_of<float>() { return CU_TENSOR_MAP_DATA_TYPE_FLOAT32; }
-
-// 3-D map over a pitched [nz][ny][px] array of T (logical extent nx), box bw x bh x 1.
-template <class T>
-inline bool encode(CUtensorMap* m, const Geom& g, void* base, int bw, int bh) {
-    auto fn = encoder();
-    if (!fn) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
-    const cuuint64_t strides[2] = {(cuuint64_t)(g.px * sizeof(T)), (cuuint64_t)(g.plane * sizeof(T))};
-    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
-    const cuuint32_t es[3] = {1, 1, 1};
-    return fn(m, dtype_of<T>(), 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 template <class S, int R>
 bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     typedef Geo<S, R> G;
