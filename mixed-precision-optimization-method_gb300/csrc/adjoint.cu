@@ -125,80 +125,94 @@ struct MemUpd {
     (void)sz;
 
 // ------------------------------------------------------------------------------------------- step^T
-// Per backward step: record^T (separate, atomic), then
-//   k_adj_a  T^T per cell: derivative-group adjoints tmpT[7] (0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz) and
-//            the T-coefficient gradients;
-//   k_gather<.., 0>  the T^T gather into lv, lq, the V-slot adjoint memory update of the previous backward
-//            step (from its tmpV at this cell), then V^T per cell: tmpV[6] (0..2 Sigma_x,y,z, 3..5 Dp_x,y,z)
-//            and the V-coefficient gradients;
-//   k_gather<.., 1>  the V^T gather into ls, lp and the T-slot adjoint memory update of this step.
-// A gather reads the adjoint memory of its own slots only, and each memory update runs after every gather
-// that reads those slots.
+// Backward step n (record^T of step n already applied to the adjoint fields, and T^T per cell of step n already
+// done: tmpT[7] (0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz) and the T-coefficient gradients):
+//   k_gather<.., 0>  the T^T gather into lv, lq, then V^T per cell: tmpV[6] (0..2 Sigma_x,y,z, 3..5 Dp_x,y,z) and
+//            the V-coefficient gradients;
+//   k_gather<.., 1>  the V^T gather into ls, lp, the T-slot adjoint memory update of step n, and (fused, n >= 1)
+//            T^T per cell of step n - 1 from the new ls, lp (tmpT of step n is read before it is overwritten);
+//   k_vmem   the V-slot adjoint memory update of step n on the slab cells (after the V^T gather that reads it);
+//   then source^T of step n and record^T of step n - 1, which also adds its injection's share to the fused T^T
+//   at the receiver cells (k_adj_recfix).  k_adj_a is T^T per cell for the first backward step only.
+// A gather reads the adjoint memory of its own slots only, and each memory update runs after every gather that
+// reads those slots.  Every kernel issues all of a cell's global loads before its first global store: the arrays
+// never alias, but the compiler cannot know that, and each store between two loads would cost a memory round
+// trip.
+
+// T^T per cell: derivative-group adjoints from the stress/pressure adjoints lt (sxx syy szz sxy sxz syz p) and the
+// coefficients kc (P1 P2 S1 S2 S3 SXYC SXZC SYZC).
+template <class A>
+__device__ __forceinline__ void t_groups(const A (&lt)[7], const A (&kc)[8], A (&o)[7]) {
+    const A lp = lt[6], lxx = lt[0], lyy = lt[1], lzz = lt[2];
+    o[0] = -kc[0] * lp + kc[3] * lxx + kc[2] * (lyy + lzz);
+    o[1] = -kc[0] * lp + kc[3] * lyy + kc[2] * (lxx + lzz);
+    o[2] = -kc[0] * lp + kc[3] * lzz + kc[2] * (lxx + lyy);
+    o[3] = -kc[1] * lp + kc[4] * (lxx + lyy + lzz);
+    o[4] = kc[5] * lt[3];
+    o[5] = kc[6] * lt[4];
+    o[6] = kc[7] * lt[5];
+}
+// T-coefficient gradient increments (P1 P2 S1 S2 S3 SXYC SXZC SYZC) from lt and the forward derivatives du
+// (uxx uyy uzz div-q uxy uyx uxz uzx uyz uzy).
+template <class A>
+__device__ __forceinline__ void t_grad(const A (&lt)[7], const A (&du)[10], A (&o)[8]) {
+    const A lp = lt[6], lxx = lt[0], lyy = lt[1], lzz = lt[2];
+    const A uxx = du[0], uyy = du[1], uzz = du[2], dq = du[3];
+    o[0] = -lp * (uxx + uyy + uzz);
+    o[1] = -lp * dq;
+    o[2] = lxx * (uyy + uzz) + lyy * (uxx + uzz) + lzz * (uxx + uyy);
+    o[3] = lxx * uxx + lyy * uyy + lzz * uzz;
+    o[4] = (lxx + lyy + lzz) * dq;
+    o[5] = lt[3] * (du[4] + du[5]);
+    o[6] = lt[4] * (du[6] + du[7]);
+    o[7] = lt[5] * (du[8] + du[9]);
+}
+// du at cell c from the forward fields vx vy vz qx qy qz (storage type, direct loads)
 template <class S, int R>
-__global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a, int first) {
+__device__ __forceinline__ void vq_derivs(const void* const (&f)[6], long long c, long long sy, long long sz,
+                                          typename Traits<S>::C (&du)[10]) {
+    typedef Adj<S, R> Q;
+    du[0] = Q::bwd(f[0], c, 1);   // uxx
+    du[1] = Q::bwd(f[1], c, sy);  // uyy
+    du[2] = Q::bwd(f[2], c, sz);  // uzz
+    du[3] = Q::bwd(f[3], c, 1) + Q::bwd(f[4], c, sy) + Q::bwd(f[5], c, sz);
+    du[4] = Q::fwd(f[0], c, sy);  // uxy
+    du[5] = Q::fwd(f[1], c, 1);   // uyx
+    du[6] = Q::fwd(f[0], c, sz);  // uxz
+    du[7] = Q::fwd(f[2], c, 1);   // uzx
+    du[8] = Q::fwd(f[1], c, sz);  // uyz
+    du[9] = Q::fwd(f[2], c, sy);  // uzy
+}
+
+// T^T per cell of the first backward step.
+template <class S, int R>
+__global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
     typedef Adj<S, R> Q;
     typedef typename Q::A A;
     CELL_INDEX
-    // Every load of the cell is issued before its first store: the arrays never alias, but the compiler cannot
-    // know that, and each store between two loads would cost one memory round trip.
-    A lt[7];  // 0 sxx, 1 syy, 2 szz, 3 sxy, 4 sxz, 5 syz, 6 p
+    A lt[7], kc[8];
 #pragma unroll
     for (int q = 0; q < 7; q++) lt[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
-    A kc[8];  // P1, P2, S1, S2, S3, SXYC, SXZC, SYZC
 #pragma unroll
     for (int q = 0; q < 8; q++) kc[q] = Q::coef(g, p, P1 + q, c);
-    const bool slab = !interior(g, i, j, k);
-    const bool gr = a.grad && !slab;
+    const bool gr = a.grad && interior(g, i, j, k);
     A du[10], go[8];
     if (gr) {
-        du[0] = Q::bwd(a.cur[BEHF_VX], c, 1);   // uxx
-        du[1] = Q::bwd(a.cur[BEHF_VY], c, sy);  // uyy
-        du[2] = Q::bwd(a.cur[BEHF_VZ], c, sz);  // uzz
-        du[3] = Q::bwd(a.cur[BEHF_QX], c, 1) + Q::bwd(a.cur[BEHF_QY], c, sy) + Q::bwd(a.cur[BEHF_QZ], c, sz);
-        du[4] = Q::fwd(a.cur[BEHF_VX], c, sy);  // uxy
-        du[5] = Q::fwd(a.cur[BEHF_VY], c, 1);   // uyx
-        du[6] = Q::fwd(a.cur[BEHF_VX], c, sz);  // uxz
-        du[7] = Q::fwd(a.cur[BEHF_VZ], c, 1);   // uzx
-        du[8] = Q::fwd(a.cur[BEHF_VY], c, sz);  // uyz
-        du[9] = Q::fwd(a.cur[BEHF_VZ], c, sy);  // uzy
+        const void* const f[6] = {a.cur[BEHF_VX], a.cur[BEHF_VY], a.cur[BEHF_VZ],
+                                  a.cur[BEHF_QX], a.cur[BEHF_QY], a.cur[BEHF_QZ]};
+        vq_derivs<S, R>(f, c, sy, sz, du);
 #pragma unroll
         for (int q = 0; q < 8; q++) go[q] = Q::ad(a.g[P1 + q])[c];
     }
-    // V-slot adjoint memory of the previous backward step: its tmpV at this cell (read by the V^T gather of that
-    // step, which has completed), on slab cells
-    const bool mem = slab && g.W > 0 && !first;
-    A tv[6];
-    MemUpd<A, 0, 0x3> mv;
-    if (mem) {
+    A tg[7];
+    t_groups(lt, kc, tg);
 #pragma unroll
-        for (int q = 0; q < 6; q++) tv[q] = Q::ad(a.tmpV[q])[c];
-        mv.load(g, p, a, i, j, k);
-    }
-    const A lp = lt[6], lxx = lt[0], lyy = lt[1], lzz = lt[2];
-    const A p1 = kc[0], p2 = kc[1], s1 = kc[2], s2 = kc[3], s3 = kc[4];
-    Q::ad(a.tmpT[0])[c] = -p1 * lp + s2 * lxx + s1 * (lyy + lzz);
-    Q::ad(a.tmpT[1])[c] = -p1 * lp + s2 * lyy + s1 * (lxx + lzz);
-    Q::ad(a.tmpT[2])[c] = -p1 * lp + s2 * lzz + s1 * (lxx + lyy);
-    Q::ad(a.tmpT[3])[c] = -p2 * lp + s3 * (lxx + lyy + lzz);
-    Q::ad(a.tmpT[4])[c] = kc[5] * lt[3];
-    Q::ad(a.tmpT[5])[c] = kc[6] * lt[4];
-    Q::ad(a.tmpT[6])[c] = kc[7] * lt[5];
+    for (int q = 0; q < 7; q++) Q::ad(a.tmpT[q])[c] = tg[q];
     if (gr) {
-        const A uxx = du[0], uyy = du[1], uzz = du[2], dq = du[3];
-        Q::ad(a.g[P1])[c] = go[0] - lp * (uxx + uyy + uzz);
-        Q::ad(a.g[P2])[c] = go[1] - lp * dq;
-        Q::ad(a.g[S1])[c] = go[2] + lxx * (uyy + uzz) + lyy * (uxx + uzz) + lzz * (uxx + uyy);
-        Q::ad(a.g[S2])[c] = go[3] + lxx * uxx + lyy * uyy + lzz * uzz;
-        Q::ad(a.g[S3])[c] = go[4] + (lxx + lyy + lzz) * dq;
-        Q::ad(a.g[SXYC])[c] = go[5] + lt[3] * (du[4] + du[5]);
-        Q::ad(a.g[SXZC])[c] = go[6] + lt[4] * (du[6] + du[7]);
-        Q::ad(a.g[SYZC])[c] = go[7] + lt[5] * (du[8] + du[9]);
-    }
-    if (mem) {
-        // axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
-        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y
-        const A D[3][4] = {{tv[0], tv[3], tv[1], tv[2]}, {tv[1], tv[4], tv[0], tv[2]}, {tv[2], tv[5], tv[0], tv[1]}};
-        mv.store(a, D);
+        A inc[8];
+        t_grad(lt, du, inc);
+#pragma unroll
+        for (int q = 0; q < 8; q++) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
     }
 }
 
@@ -262,10 +276,11 @@ struct G25 {
 // Shared memory of a gather CTA: NS = 2 stages of [4 x windows][4 y windows] (adjoint arrays, type A), then the
 // z ring [4][ZS] of row boxes.  x windows start at the 16-byte aligned column i0 - R = 32 bx, padded to whole
 // 16-byte chunks (XWP); y windows and ring rows start at i0 = R + 32 bx when that is 16-byte aligned (YV), else at
-// i0 - R with the x window's width (YC = column of i0 in them).  With SNAP (the T^T gather of the 16-bit kinds)
-// each stage also holds [4 x][4 y] windows of the forward snapshot (type S: sxx sxy sxz p / syy sxy syz p) and a
-// second ring holds its z rows (szz sxz syz p), for the stencils of the V-coefficient gradients.  Every box starts
-// on a 128-byte boundary.
+// i0 - R with the x window's width (YC = column of i0 in them).  With SNAP (the 16-bit kinds) each stage also
+// holds [4 x][4 y] windows of forward snapshot fields (type S) and a second ring holds their z rows, for the
+// stencils of the coefficient gradients: KIND 0 stresses and pressure of step n (x: sxx sxy sxz p, y: syy sxy
+// syz p, z: szz sxz syz p), KIND 1 velocities and Darcy velocities of step n - 1 (x: vx vy vz qx, y: vy vx vz qy,
+// z: vz vx vy qz).  Every box starts on a 128-byte boundary.
 template <class S, int R, int KIND>
 struct GMap {
     typedef typename Traits<S>::C A;
@@ -276,7 +291,7 @@ struct GMap {
     static constexpr bool YV = (R * (int)sizeof(A)) % 16 == 0;
     static constexpr int YW = YV ? GX : XWP;
     static constexpr int YC = YV ? 0 : R;
-    static constexpr bool SNAP = KIND == 0 && sizeof(S) == 2;
+    static constexpr bool SNAP = sizeof(S) == 2;
     static constexpr int CHS = 16 / (int)sizeof(S);
     static constexpr int XWPS = (XW + CHS - 1) / CHS * CHS;
     static constexpr bool YVS = (R * (int)sizeof(S)) % 16 == 0;
@@ -304,13 +319,14 @@ struct GMap {
 // KIND 0: T^T gather (X: T0 s4, T4 s6h, T5 s7h, T3 s5;  Y: T1 s4, T4 s6h, T6 s7h, T3 s5;
 //                      Z: T2 s4, T5 s6h, T6 s7h, T3 s5), then V^T per cell.
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
-//                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update.
+//                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update and, with fuse, T^T per
+//                      cell of step n - 1.
 // maps.m[0..3]: x windows, [4..7]: y windows, [8..11]: ring rows, in the order above; smaps: the same for the
-// snapshot arrays of this step (SNAP only).
+// snapshot arrays (SNAP only).
 template <class S, int R, int KIND>
 __global__ void __launch_bounds__(256, 2)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
-             AdjPtrs a, StageSet ss, int zc) {
+             AdjPtrs a, StageSet ss, int zc, int fuse) {
     typedef G25<S, R> W;
     typedef Adj<S, R> Q;
     typedef GMap<S, R, KIND> M;
@@ -338,8 +354,8 @@ __global__ void __launch_bounds__(256, 2)
     const int yx0s = M::YVS ? i0 : i0 - R;   // the same for the snapshot
     // the snapshot is staged only where the tile and z range hold cells outside every CPML slab
     auto has_int = [&](int lo, int hi, int n) { return g.W == 0 || max(lo, g.L) <= min(hi, n - 2 - g.L); };
-    const bool snap = M::SNAP && a.grad && has_int(i0, i0 + GX - 1, g.nx) && has_int(j0, j0 + GY - 1, g.ny) &&
-                      has_int(kb, ke - 1, g.nz);
+    const bool snap = M::SNAP && a.grad && (KIND == 0 || fuse) && has_int(i0, i0 + GX - 1, g.nx) &&
+                      has_int(j0, j0 + GY - 1, g.ny) && has_int(kb, ke - 1, g.nz);
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
@@ -582,18 +598,74 @@ __global__ void __launch_bounds__(256, 2)
                     for (int q = 0; q < 7; q++) tt[q] = Q::ad(a.tmpT[q])[c];
                     mt.load(g, p, a, i, j, k);
                 }
-                Q::ad(a.lf[BEHF_SXX])[c] = lo[0] - W::bwd(WX(0));
-                Q::ad(a.lf[BEHF_SYY])[c] = lo[1] - W::bwd(WY(0));
-                Q::ad(a.lf[BEHF_SZZ])[c] = lo[2] - W::bwd(WZ(0));
-                Q::ad(a.lf[BEHF_SXY])[c] = lo[3] - (W::fwd(WY(1)) + W::fwd(WX(1)));
-                Q::ad(a.lf[BEHF_SXZ])[c] = lo[4] - (W::fwd(WZ(1)) + W::fwd(WX(2)));
-                Q::ad(a.lf[BEHF_SYZ])[c] = lo[5] - (W::fwd(WZ(2)) + W::fwd(WY(2)));
-                Q::ad(a.lf[BEHF_P])[c] = lo[6] - (W::bwd(WX(3)) + W::bwd(WY(3)) + W::bwd(WZ(3)));
+                // T^T per cell of step n - 1 (fuse): coefficients, and on cells outside the slabs the forward
+                // derivatives of step n - 1 and the gradient accumulators
+                A kc[8];
+                if (fuse) {
+#pragma unroll
+                    for (int q = 0; q < 8; q++) kc[q] = Q::coef(g, p, P1 + q, c);
+                }
+                const bool gr = fuse && a.grad && !mem;
+                A du[10], go[8];
+                if (gr) {
+                    if constexpr (M::SNAP) {  // from the staged windows (gr implies snap)
+                        constexpr int XES = M::XBOXS / (int)sizeof(S), YES = M::YBOXS / (int)sizeof(S);
+                        constexpr int ZES = M::ZBOXS / (int)sizeof(S);
+                        const S* xs = XS(st, 0) + ty * M::XWPS + tx + R;
+                        const S* ys = YS(st, 0) + (ty + R) * M::YWS + M::YCS + tx;
+                        const S* zsb = ZS_(0, 0) + ty * M::YWS + M::YCS + tx;
+                        const int zs0 = (k - R) % M::ZS;
+                        auto zsl = [&](int d) { return zs0 + R + d >= M::ZS ? zs0 + R + d - M::ZS : zs0 + R + d; };
+#define SXW(q) [&](int d) { return Q::ls(xs, (q) * XES + d); }
+#define SYW(q) [&](int d) { return Q::ls(ys, (q) * YES + d * M::YWS); }
+#define SZW(q) [&](int d) { return Q::ls(zsb, ((q) * M::ZS + zsl(d)) * ZES); }
+                        // x: vx vy vz qx;  y: vy vx vz qy;  z: vz vx vy qz
+                        du[0] = W::bwd(SXW(0));                                   // uxx
+                        du[1] = W::bwd(SYW(0));                                   // uyy
+                        du[2] = W::bwd(SZW(0));                                   // uzz
+                        du[3] = W::bwd(SXW(3)) + W::bwd(SYW(3)) + W::bwd(SZW(3));  // div q
+                        du[4] = W::fwd(SYW(1));                                   // uxy
+                        du[5] = W::fwd(SXW(1));                                   // uyx
+                        du[6] = W::fwd(SZW(1));                                   // uxz
+                        du[7] = W::fwd(SXW(2));                                   // uzx
+                        du[8] = W::fwd(SZW(2));                                   // uyz
+                        du[9] = W::fwd(SYW(2));                                   // uzy
+#undef SXW
+#undef SYW
+#undef SZW
+                    } else {
+                        vq_derivs<S, R>(a.vq1, c, sy, sz, du);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; q++) go[q] = Q::ad(a.g[P1 + q])[c];
+                }
+                A lt[7];
+                lt[0] = lo[0] - W::bwd(WX(0));
+                lt[1] = lo[1] - W::bwd(WY(0));
+                lt[2] = lo[2] - W::bwd(WZ(0));
+                lt[3] = lo[3] - (W::fwd(WY(1)) + W::fwd(WX(1)));
+                lt[4] = lo[4] - (W::fwd(WZ(1)) + W::fwd(WX(2)));
+                lt[5] = lo[5] - (W::fwd(WZ(2)) + W::fwd(WY(2)));
+                lt[6] = lo[6] - (W::bwd(WX(3)) + W::bwd(WY(3)) + W::bwd(WZ(3)));
+#pragma unroll
+                for (int q = 0; q < 7; q++) Q::ad(a.lf[BEHF_SXX + q])[c] = lt[q];
                 if (mem) {
                     // axis x: uxx s4, wx s5, uyx s6h, uzx s7h; y: uyy, wy, uxy, uzy; z: uzz, wz, uxz, uyz
                     const A D[3][4] = {{tt[0], tt[3], tt[4], tt[5]}, {tt[1], tt[3], tt[4], tt[6]},
                                        {tt[2], tt[3], tt[5], tt[6]}};
                     mt.store(a, D);
+                }
+                if (fuse) {
+                    A tg[7];
+                    t_groups(lt, kc, tg);
+#pragma unroll
+                    for (int q = 0; q < 7; q++) Q::ad(a.tmpT[q])[c] = tg[q];
+                }
+                if (gr) {
+                    A inc[8];
+                    t_grad(lt, du, inc);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
                 }
             }
 #undef WX
@@ -616,6 +688,61 @@ __global__ void __launch_bounds__(256, 2)
 
 #undef CELL_INDEX
 
+// V-slot adjoint memory update of one step on the slab cells of the updated region, one slab cell of one axis per
+// thread (a cell in two slabs is visited once per axis): from the cell's tmpV, the slots 0..3 of that axis.
+__device__ __forceinline__ int slab_pos(int s, int n, int L) { return s < L ? s : n - 1 - L + (s - L); }
+template <class A>
+__global__ void k_vmem(Geom g, DevPtrs p, AdjPtrs a) {
+    const long long n0 = (long long)g.nz * g.ny * g.W, n1 = (long long)g.nz * g.W * g.nx;
+    const long long n2 = (long long)g.W * g.ny * g.nx, tot = n0 + n1 + n2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        int ax, i, j, k, pos;
+        long long u = t;
+        if (u < n0) {  // x slab [nz][ny][W]
+            ax = 0;
+            const int sl = (int)(u % g.W);
+            const long long r = u / g.W;
+            j = (int)(r % g.ny);
+            k = (int)(r / g.ny);
+            i = pos = slab_pos(sl, g.nx, g.L);
+        } else if ((u -= n0) < n1) {  // y slab [nz][W][nx]
+            ax = 1;
+            i = (int)(u % g.nx);
+            const long long r = u / g.nx;
+            k = (int)(r / g.W);
+            j = pos = slab_pos((int)(r % g.W), g.ny, g.L);
+        } else {  // z slab [W][ny][nx]
+            u -= n1;
+            ax = 2;
+            i = (int)(u % g.nx);
+            const long long r = u / g.nx;
+            j = (int)(r % g.ny);
+            k = pos = slab_pos((int)(r / g.ny), g.nz, g.L);
+        }
+        if (i < g.R || i >= g.nx - g.R || j < g.R || j >= g.ny - g.R || k < g.R || k >= g.nz - g.R) continue;
+        const long long c = (long long)k * g.plane + (long long)j * g.px + i;
+        // axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
+        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y
+        const int dq[4] = {ax, ax + 3, ax == 0 ? 1 : 0, ax == 2 ? 1 : 2};
+        A D[4], L[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            D[q] = reinterpret_cast<const A*>(a.tmpV[dq[q]])[c];
+            L[q] = reinterpret_cast<const A*>(a.lpsi[ax][q])[u];
+        }
+        const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
+        const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const A Ap = q < 2 ? pa2 : pa, B = q < 2 ? pb2 : pb;
+            const A Lm = L[q] + D[q];
+            reinterpret_cast<A*>(a.lpsi[ax][q])[u] = Ap * Lm;
+            reinterpret_cast<A*>(a.lprv[ax][q])[u] = Ap * B * Lm;
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------- record^T, source^T
 template <class A>
 __global__ void k_adj_record(AdjPtrs a, const long long* off, const int* comp, int nrec, const double* adj, int nt,
@@ -624,6 +751,39 @@ __global__ void k_adj_record(AdjPtrs a, const long long* off, const int* comp, i
     if (r >= nrec) return;
     const int q = comp[r];
     atomicAdd(reinterpret_cast<A*>(a.lf[q]) + off[r], (A)(adj[(long long)r * nt + it] * sc.s[q]));
+}
+
+// record^T of step n - 1 after the fused T^T of that step: the injection into the adjoint fields, plus its share of
+// tmpT and of the T-coefficient gradients at the receiver cell (atomic: receivers may share a cell).
+template <class S, int R>
+__global__ void k_adj_recfix(Geom g, DevPtrs p, AdjPtrs a, const long long* off, const int* comp, int nrec,
+                             const double* adj, int nt, int it, AdjScales sc) {
+    typedef Adj<S, R> Q;
+    typedef typename Q::A A;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const int q = comp[r];
+    const long long c = off[r];
+    const A dv = (A)(adj[(long long)r * nt + it] * sc.s[q]);
+    atomicAdd(reinterpret_cast<A*>(a.lf[q]) + c, dv);
+    if (q < BEHF_SXX) return;  // velocity receivers: V^T reads lv directly
+    const int k = (int)(c / g.plane), j = (int)((c % g.plane) / g.px), i = (int)(c % g.px);
+    if (i < R || i >= g.nx - R || j < R || j >= g.ny - R || k < R || k >= g.nz - R) return;
+    A lt[7], kc[8], tg[7];
+#pragma unroll
+    for (int u = 0; u < 7; u++) lt[u] = u == q - BEHF_SXX ? dv : (A)0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) kc[u] = Q::coef(g, p, P1 + u, c);
+    t_groups(lt, kc, tg);
+#pragma unroll
+    for (int u = 0; u < 7; u++) atomicAdd(Q::ad(a.tmpT[u]) + c, tg[u]);
+    if (a.grad && interior(g, i, j, k)) {
+        A du[10], inc[8];
+        vq_derivs<S, R>(a.vq1, c, g.px, g.plane, du);
+        t_grad(lt, du, inc);
+#pragma unroll
+        for (int u = 0; u < 8; u++) atomicAdd(Q::ad(a.g[P1 + u]) + c, inc[u]);
+    }
 }
 
 template <class A>
@@ -736,12 +896,19 @@ __global__ void k_grad_moduli(GradModArgs a) {
 }
 
 template <class S, int R>
-cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap, int first,
-                  cudaStream_t st) {
+cudaError_t adj_first_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
     const dim3 block(32, 8, 1);
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
     const dim3 grid((nxu + 31) / 32, (nyu + 7) / 8, nzu);
-    k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a, first);
+    k_adj_a<S, R><<<grid, block, 0, st>>>(g, p, a);
+    return cudaGetLastError();
+}
+
+template <class S, int R>
+cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snapT,
+                  const GatherMaps* snapV, int fuse, cudaStream_t st) {
+    const dim3 block(32, 8, 1);
+    const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
     // gathers: z chunks so that about eight CTAs per SM are launched
     static int sms = 0;
     if (sms == 0) {
@@ -776,9 +943,19 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    if (GMap<S, R, 0>::SNAP && a.grad && !snap) return cudaErrorInvalidValue;
-    k_gather<S, R, 0><<<ggrid, block, smem0, st>>>(m.t, snap ? *snap : m.t, g, p, a, t, zc);
-    k_gather<S, R, 1><<<ggrid, block, smem1, st>>>(m.v, m.v, g, p, a, v, zc);
+    if (GMap<S, R, 0>::SNAP && a.grad && (!snapT || (fuse && !snapV))) return cudaErrorInvalidValue;
+    k_gather<S, R, 0><<<ggrid, block, smem0, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0);
+    k_gather<S, R, 1><<<ggrid, block, smem1, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse);
+    if (g.W > 0) {
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (sms <= 0) sms = 148;
+        }
+        k_vmem<typename Traits<S>::C><<<sms * 8, 256, 0, st>>>(g, p, a);
+    }
     return cudaGetLastError();
 }
 
@@ -812,14 +989,19 @@ cudaError_t build_maps_r(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
 }
 
 template <class S, int R>
-cudaError_t build_snap_maps_r(const Geom& g, void* const f[kNField], GatherMaps* m) {
+cudaError_t build_snap_maps_r(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv) {
     typedef GMap<S, R, 0> M;
     if (!M::SNAP) return cudaSuccess;
     if (!tiled::encoder()) return cudaErrorNotSupported;
     void* const x[4] = {f[BEHF_SXX], f[BEHF_SXY], f[BEHF_SXZ], f[BEHF_P]};
     void* const y[4] = {f[BEHF_SYY], f[BEHF_SXY], f[BEHF_SYZ], f[BEHF_P]};
     void* const z[4] = {f[BEHF_SZZ], f[BEHF_SXZ], f[BEHF_SYZ], f[BEHF_P]};
-    return build_gather_maps<S, M::XWPS, M::YWS, M::YH>(g, x, y, z, m) ? cudaSuccess : cudaErrorInvalidValue;
+    void* const vx[4] = {f[BEHF_VX], f[BEHF_VY], f[BEHF_VZ], f[BEHF_QX]};
+    void* const vy[4] = {f[BEHF_VY], f[BEHF_VX], f[BEHF_VZ], f[BEHF_QY]};
+    void* const vz[4] = {f[BEHF_VZ], f[BEHF_VX], f[BEHF_VY], f[BEHF_QZ]};
+    const bool ok = build_gather_maps<S, M::XWPS, M::YWS, M::YH>(g, x, y, z, mt) &&
+                    build_gather_maps<S, M::XWPS, M::YWS, M::YH>(g, vx, vy, vz, mv);
+    return ok ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -839,25 +1021,49 @@ bool adj_snap_staged() {
     return sizeof(S) == 2;
 }
 template <class S>
-cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* m) {
+cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv) {
     switch (g.R) {
-        case 1: return build_snap_maps_r<S, 1>(g, f, m);
-        case 2: return build_snap_maps_r<S, 2>(g, f, m);
-        case 3: return build_snap_maps_r<S, 3>(g, f, m);
-        case 4: return build_snap_maps_r<S, 4>(g, f, m);
+        case 1: return build_snap_maps_r<S, 1>(g, f, mt, mv);
+        case 2: return build_snap_maps_r<S, 2>(g, f, mt, mv);
+        case 3: return build_snap_maps_r<S, 3>(g, f, mt, mv);
+        case 4: return build_snap_maps_r<S, 4>(g, f, mt, mv);
     }
     return cudaErrorInvalidValue;
 }
 template <class S>
-cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap,
-                     int first, cudaStream_t st) {
+cudaError_t adj_first(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st) {
     switch (g.R) {
-        case 1: return adj_r<S, 1>(g, p, a, m, snap, first, st);
-        case 2: return adj_r<S, 2>(g, p, a, m, snap, first, st);
-        case 3: return adj_r<S, 3>(g, p, a, m, snap, first, st);
-        case 4: return adj_r<S, 4>(g, p, a, m, snap, first, st);
+        case 1: return adj_first_r<S, 1>(g, p, a, st);
+        case 2: return adj_first_r<S, 2>(g, p, a, st);
+        case 3: return adj_first_r<S, 3>(g, p, a, st);
+        case 4: return adj_first_r<S, 4>(g, p, a, st);
     }
     return cudaErrorInvalidValue;
+}
+template <class S>
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snapT,
+                     const GatherMaps* snapV, int fuse, cudaStream_t st) {
+    switch (g.R) {
+        case 1: return adj_r<S, 1>(g, p, a, m, snapT, snapV, fuse, st);
+        case 2: return adj_r<S, 2>(g, p, a, m, snapT, snapV, fuse, st);
+        case 3: return adj_r<S, 3>(g, p, a, m, snapT, snapV, fuse, st);
+        case 4: return adj_r<S, 4>(g, p, a, m, snapT, snapV, fuse, st);
+    }
+    return cudaErrorInvalidValue;
+}
+template <class S>
+cudaError_t adj_recfix(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const long long* off, const int* comp,
+                       int nrec, const double* adj, int nt, int it, const AdjScales& sc, cudaStream_t st) {
+    if (nrec <= 0) return cudaSuccess;
+    const int nb = (nrec + 255) / 256;
+    switch (g.R) {
+        case 1: k_adj_recfix<S, 1><<<nb, 256, 0, st>>>(g, p, a, off, comp, nrec, adj, nt, it, sc); break;
+        case 2: k_adj_recfix<S, 2><<<nb, 256, 0, st>>>(g, p, a, off, comp, nrec, adj, nt, it, sc); break;
+        case 3: k_adj_recfix<S, 3><<<nb, 256, 0, st>>>(g, p, a, off, comp, nrec, adj, nt, it, sc); break;
+        case 4: k_adj_recfix<S, 4><<<nb, 256, 0, st>>>(g, p, a, off, comp, nrec, adj, nt, it, sc); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 template <class S>
 cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, int nrec, const double* adj, int nt,
@@ -884,9 +1090,13 @@ cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st) {
 #define BEHF_ADJ_INST(S)                                                                                         \
     template cudaError_t adj_build_maps<S>(const Geom&, const AdjPtrs&, AdjMaps*);                             \
     template bool adj_snap_staged<S>();                                                                        \
-    template cudaError_t adj_build_snap_maps<S>(const Geom&, void* const*, GatherMaps*);                       \
+    template cudaError_t adj_build_snap_maps<S>(const Geom&, void* const*, GatherMaps*, GatherMaps*);          \
+    template cudaError_t adj_first<S>(const Geom&, const DevPtrs&, const AdjPtrs&, cudaStream_t);              \
     template cudaError_t adj_step<S>(const Geom&, const DevPtrs&, const AdjPtrs&, const AdjMaps&,              \
-                                     const GatherMaps*, int, cudaStream_t);                                    \
+                                     const GatherMaps*, const GatherMaps*, int, cudaStream_t);                 \
+    template cudaError_t adj_recfix<S>(const Geom&, const DevPtrs&, const AdjPtrs&, const long long*,          \
+                                       const int*, int, const double*, int, int, const AdjScales&,             \
+                                       cudaStream_t);                                                          \
     template cudaError_t adj_record<S>(const AdjPtrs&, const long long*, const int*, int, const double*, int, int, \
                                        const AdjScales&, cudaStream_t);                                          \
     template cudaError_t adj_point<S>(const AdjPtrs&, long long, int, double, const float*, int, int, double*,  \

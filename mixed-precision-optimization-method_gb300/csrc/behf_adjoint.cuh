@@ -27,6 +27,7 @@ struct AdjPtrs {
     void* g[kNCoef];         // gradient accumulators per effective coefficient, type A, pitched
     const void* cur[kNField];  // forward snapshot of this step after V (and the force source), type S
     const void* qprev[3];    // q before V of this step, type S
+    const void* vq1[6];      // vx vy vz qx qy qz after V of step n - 1 (the fused T^T of that step), type S
     int grad;                // accumulate coefficient gradients
 };
 
@@ -47,17 +48,27 @@ struct AdjScales {
 // tensor-map encoder).
 template <class S>
 cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m);
-// The T^T gather of the 16-bit kinds stages the forward snapshot of the step (its stress and pressure stencils
-// for the V-coefficient gradients) through tensor maps built per snapshot buffer by adj_build_snap_maps.
+// The gathers of the 16-bit kinds stage forward snapshot fields for the coefficient-gradient stencils through
+// tensor maps built per snapshot buffer by adj_build_snap_maps: mt over its stresses and pressure (the T^T gather
+// of the step), mv over its velocities and Darcy velocities (the fused T^T of the step before).
 template <class S>
 bool adj_snap_staged();
 template <class S>
-cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* m);
-// T^T and V^T of one step (three launches); first = 1 on the first backward step (no V-slot memory pending);
-// snap: the maps of a.cur (required when adj_snap_staged<S>() and a.grad, else ignored).
+cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv);
+// T^T per cell of the first backward step (after its record^T).
 template <class S>
-cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snap,
-                     int first, cudaStream_t st);
+cudaError_t adj_first(const Geom& g, const DevPtrs& p, const AdjPtrs& a, cudaStream_t st);
+// Backward step n with T^T per cell of step n done: the T^T gather + V^T, the V^T gather + T-slot memory update
+// (+ T^T per cell of step n - 1 with fuse = 1, from a.vq1), the V-slot memory update.  snapT / snapV: the maps of
+// a.cur and of the snapshot of step n - 1 (required when adj_snap_staged<S>() and a.grad, else ignored).
+template <class S>
+cudaError_t adj_step(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMaps& m, const GatherMaps* snapT,
+                     const GatherMaps* snapV, int fuse, cudaStream_t st);
+// record^T of step it after a fused T^T of that step: adj_record plus its share of tmpT and of the T-coefficient
+// gradients at the receiver cells.
+template <class S>
+cudaError_t adj_recfix(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const long long* off, const int* comp,
+                       int nrec, const double* adj, int nt, int it, const AdjScales& sc, cudaStream_t st);
 // record^T: lf[comp[r]][off[r]] += adj[r * nt + it] * sc.s[comp[r]]  (atomic: receivers may share a cell)
 template <class S>
 cudaError_t adj_record(const AdjPtrs& a, const long long* off, const int* comp, int nrec, const double* adj, int nt,

@@ -1054,14 +1054,16 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     if (!maps) return fail(BEHF_ERR_ALLOC, "host allocation of the adjoint tensor maps");
     std::unique_ptr<AdjMaps, void (*)(void*)> maps_owner(maps, std::free);
     CK(adj_build_maps<S>(g, a, maps));
-    // tensor maps of every snapshot buffer (slot u holds the fields after V of step s0 + u - 1)
-    std::vector<GatherMaps> snap_maps;
+    // tensor maps of every snapshot buffer (slot u holds the fields after V of step s0 + u - 1; slot 0 the state
+    // after step s0 - 1, whose velocities and Darcy velocities are those after its V)
+    std::vector<GatherMaps> snap_mt, snap_mv;
     if (adj_snap_staged<S>()) {
-        snap_maps.resize(S_ + 1);
+        snap_mt.resize(S_ + 1);
+        snap_mv.resize(S_ + 1);
         for (int u = 0; u <= S_; u++) {
             void* f[kNField];
             for (int q = 0; q < kNField; q++) f[q] = snap + snap_bytes * u + (size_t)q * align256(nf * c->es);
-            CK(adj_build_snap_maps<S>(g, f, &snap_maps[u]));
+            CK(adj_build_snap_maps<S>(g, f, &snap_mt[u], &snap_mv[u]));
         }
     }
 
@@ -1151,14 +1153,24 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             CK(aux_tick(c->d_it, 1, c->stream));
             c->launches += 4;
         }
+        // backward step it: T^T per cell of it is done (the first step: here, after its record^T; later steps: fused
+        // into the V^T gather of step it + 1, completed by the record^T of it)
         for (int it = s1 - 1; it >= s0; it--) {
             for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(it - s0 + 1, f);
             for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(it - s0, BEHF_QX + d);
-            CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
-            CK(adj_step<S>(g, c->p, a, *maps, snap_maps.empty() ? nullptr : &snap_maps[it - s0 + 1],
-                           it == nt - 1 ? 1 : 0, c->stream));
+            for (int d = 0; d < 6; d++) a.vq1[d] = snap_ptr(it - s0, BEHF_VX + d);
+            if (it == nt - 1) {
+                CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
+                CK(adj_first<S>(g, c->p, a, c->stream));
+                c->launches += 2;
+            }
+            const int fuse = it >= 1 ? 1 : 0;
+            const bool sm = !snap_mt.empty();
+            CK(adj_step<S>(g, c->p, a, *maps, sm ? &snap_mt[it - s0 + 1] : nullptr, sm ? &snap_mv[it - s0] : nullptr,
+                           fuse, c->stream));
             CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
-            c->launches += 5;
+            if (fuse) CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc, c->stream));
+            c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse;
         }
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
