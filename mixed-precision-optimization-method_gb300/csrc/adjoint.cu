@@ -183,6 +183,26 @@ __device__ __forceinline__ void vq_derivs(const void* const (&f)[6], long long c
     du[8] = Q::fwd(f[1], c, sz);  // uyz
     du[9] = Q::fwd(f[2], c, sy);  // uzy
 }
+// The T coefficients at c; with a.derived (the forward ran the tiled kernels, which use S3 = P1 c_s3 instead of
+// the stored S3) the derived S3.
+template <class S, int R>
+__device__ __forceinline__ void t_coefs(const Geom& g, const DevPtrs& p, const AdjPtrs& a, long long c,
+                                        typename Traits<S>::C (&kc)[8]) {
+    typedef Adj<S, R> Q;
+    typedef typename Q::A A;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        if (q != 4) kc[q] = Q::coef(g, p, P1 + q, c);
+    kc[4] = a.derived ? kc[0] * (A)g.c_s3 : Q::coef(g, p, S3, c);
+}
+// With a.derived the S3 gradient belongs to P1 (chain rule through S3 = P1 c_s3); the S3 accumulator is unused.
+template <class A>
+__device__ __forceinline__ void t_grad_fold(const Geom& g, const AdjPtrs& a, A (&inc)[8]) {
+    if (a.derived) {
+        inc[0] += (A)g.c_s3 * inc[4];
+        inc[4] = 0;
+    }
+}
 
 // T^T per cell of the first backward step.
 template <class S, int R>
@@ -193,8 +213,7 @@ __global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
     A lt[7], kc[8];
 #pragma unroll
     for (int q = 0; q < 7; q++) lt[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
-#pragma unroll
-    for (int q = 0; q < 8; q++) kc[q] = Q::coef(g, p, P1 + q, c);
+    t_coefs<S, R>(g, p, a, c, kc);
     const bool gr = a.grad && interior(g, i, j, k);
     A du[10], go[8];
     if (gr) {
@@ -202,7 +221,7 @@ __global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
                                   a.cur[BEHF_QX], a.cur[BEHF_QY], a.cur[BEHF_QZ]};
         vq_derivs<S, R>(f, c, sy, sz, du);
 #pragma unroll
-        for (int q = 0; q < 8; q++) go[q] = Q::ad(a.g[P1 + q])[c];
+        for (int q = 0; q < 8; q++) go[q] = (q == 4 && a.derived) ? (A)0 : Q::ad(a.g[P1 + q])[c];
     }
     A tg[7];
     t_groups(lt, kc, tg);
@@ -211,8 +230,10 @@ __global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
     if (gr) {
         A inc[8];
         t_grad(lt, du, inc);
+        t_grad_fold(g, a, inc);
 #pragma unroll
-        for (int q = 0; q < 8; q++) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
+        for (int q = 0; q < 8; q++)
+            if (q != 4 || !a.derived) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
     }
 }
 
@@ -498,7 +519,7 @@ __global__ void __launch_bounds__(256, 2)
             // Each cell issues all its global loads before its first global store (see k_adj_a).
             if (KIND == 0) {
                 // V^T at this cell with lv = lv_old - dl[0..2], lq' = lq_old - dl[3..5]
-                A lvo[3], lqo[3], vu2[3], vw1[3], vu1[3], vw2[3], vw3[3];
+                A lvo[3], lqo[3], vu2[3], vw1[3], vu1[3], vw2[3], vw3[3], vw3p;
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
                     lvo[d] = Q::ad(a.lf[BEHF_VX + d])[c];
@@ -506,9 +527,11 @@ __global__ void __launch_bounds__(256, 2)
                     vu2[d] = Q::coef(g, p, VU2X + d, c);
                     vw1[d] = Q::vw1(p, d, c);
                     vu1[d] = Q::coef(g, p, VU1X + d, c);
-                    vw2[d] = Q::coef(g, p, VW2X + d, c);
-                    vw3[d] = Q::coef(g, p, (d == 2 && g.bug) ? VW3Y : VW3X + d, c);  // reference: vz uses VW3y
+                    vw3[d] = Q::coef(g, p, VW3X + d, c);
+                    // with a.derived (tiled forward) VW2 = VU2 VW3 c_vw2 with the cell's own-axis VW3
+                    vw2[d] = a.derived ? vu2[d] * vw3[d] * (A)g.c_vw2 : Q::coef(g, p, VW2X + d, c);
                 }
+                vw3p = g.bug ? Q::coef(g, p, VW3Y, c) : vw3[2];  // reference: the dp term of vz uses VW3y
                 const bool gr = a.grad && interior(g, i, j, k);
                 A sum[3], dp[3], qo[3], qn[3], go[15];
                 if (gr) {
@@ -550,7 +573,8 @@ __global__ void __launch_bounds__(256, 2)
                         qn[d] = Q::ls(a.cur[BEHF_QX + d], c);
                     }
 #pragma unroll
-                    for (int q = 0; q < 15; q++) go[q] = Q::ad(a.g[q])[c];
+                    for (int q = 0; q < 15; q++)
+                        go[q] = (a.derived && q >= VW2X && q <= VW2Z) ? (A)0 : Q::ad(a.g[q])[c];
                 }
                 A dl[6];
                 dl[0] = W::fwd(WX(0)) + W::bwd(WY(1)) + W::bwd(WZ(1));
@@ -568,13 +592,19 @@ __global__ void __launch_bounds__(256, 2)
                     Q::ad(a.lf[BEHF_VX + d])[c] = lv[d];
                     Q::ad(a.lf[BEHF_QX + d])[c] = vw1[d] * mu[d] + vu2[d] * lv[d];
                     Q::ad(a.tmpV[d])[c] = vu1[d] * lv[d] - vw2[d] * mu[d];
-                    Q::ad(a.tmpV[3 + d])[c] = -vw3[d] * mu[d];
+                    Q::ad(a.tmpV[3 + d])[c] = -(d == 2 ? vw3p : vw3[d]) * mu[d];
                 }
                 if (gr) {
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         go[VW1X + d] += mu[d] * qo[d];
-                        go[VW2X + d] += -mu[d] * sum[d];
+                        const A gw2 = -mu[d] * sum[d];
+                        if (a.derived) {  // chain rule through VW2 = VU2 VW3 c_vw2
+                            go[VU2X + d] += gw2 * vw3[d] * (A)g.c_vw2;
+                            go[VW3X + d] += gw2 * vu2[d] * (A)g.c_vw2;
+                        } else {
+                            go[VW2X + d] += gw2;
+                        }
                         go[VU1X + d] += lv[d] * sum[d];
                         go[VU2X + d] += -lv[d] * (qn[d] - qo[d]);
                     }
@@ -583,7 +613,8 @@ __global__ void __launch_bounds__(256, 2)
                     go[VW3Y] += -mu[1] * dp[1] + (g.bug ? w3z : (A)0);
                     go[VW3Z] += g.bug ? (A)0 : w3z;
 #pragma unroll
-                    for (int q = 0; q < 15; q++) Q::ad(a.g[q])[c] = go[q];
+                    for (int q = 0; q < 15; q++)
+                        if (!(a.derived && q >= VW2X && q <= VW2Z)) Q::ad(a.g[q])[c] = go[q];
                 }
             } else {
                 A lo[7];  // sxx syy szz sxy sxz syz p
@@ -601,10 +632,7 @@ __global__ void __launch_bounds__(256, 2)
                 // T^T per cell of step n - 1 (fuse): coefficients, and on cells outside the slabs the forward
                 // derivatives of step n - 1 and the gradient accumulators
                 A kc[8];
-                if (fuse) {
-#pragma unroll
-                    for (int q = 0; q < 8; q++) kc[q] = Q::coef(g, p, P1 + q, c);
-                }
+                if (fuse) t_coefs<S, R>(g, p, a, c, kc);
                 const bool gr = fuse && a.grad && !mem;
                 A du[10], go[8];
                 if (gr) {
@@ -637,7 +665,7 @@ __global__ void __launch_bounds__(256, 2)
                         vq_derivs<S, R>(a.vq1, c, sy, sz, du);
                     }
 #pragma unroll
-                    for (int q = 0; q < 8; q++) go[q] = Q::ad(a.g[P1 + q])[c];
+                    for (int q = 0; q < 8; q++) go[q] = (q == 4 && a.derived) ? (A)0 : Q::ad(a.g[P1 + q])[c];
                 }
                 A lt[7];
                 lt[0] = lo[0] - W::bwd(WX(0));
@@ -664,8 +692,10 @@ __global__ void __launch_bounds__(256, 2)
                 if (gr) {
                     A inc[8];
                     t_grad(lt, du, inc);
+                    t_grad_fold(g, a, inc);
 #pragma unroll
-                    for (int q = 0; q < 8; q++) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
+                    for (int q = 0; q < 8; q++)
+                        if (q != 4 || !a.derived) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
                 }
             }
 #undef WX
@@ -772,8 +802,7 @@ __global__ void k_adj_recfix(Geom g, DevPtrs p, AdjPtrs a, const long long* off,
     A lt[7], kc[8], tg[7];
 #pragma unroll
     for (int u = 0; u < 7; u++) lt[u] = u == q - BEHF_SXX ? dv : (A)0;
-#pragma unroll
-    for (int u = 0; u < 8; u++) kc[u] = Q::coef(g, p, P1 + u, c);
+    t_coefs<S, R>(g, p, a, c, kc);
     t_groups(lt, kc, tg);
 #pragma unroll
     for (int u = 0; u < 7; u++) atomicAdd(Q::ad(a.tmpT[u]) + c, tg[u]);
@@ -781,8 +810,10 @@ __global__ void k_adj_recfix(Geom g, DevPtrs p, AdjPtrs a, const long long* off,
         A du[10], inc[8];
         vq_derivs<S, R>(a.vq1, c, g.px, g.plane, du);
         t_grad(lt, du, inc);
+        t_grad_fold(g, a, inc);
 #pragma unroll
-        for (int u = 0; u < 8; u++) atomicAdd(Q::ad(a.g[P1 + u]) + c, inc[u]);
+        for (int u = 0; u < 8; u++)
+            if (u != 4 || !a.derived) atomicAdd(Q::ad(a.g[P1 + u]) + c, inc[u]);
     }
 }
 

@@ -29,6 +29,8 @@ struct AdjPtrs {
     const void* qprev[3];    // q before V of this step, type S
     const void* vq1[6];      // vx vy vz qx qy qz after V of step n - 1 (the fused T^T of that step), type S
     int grad;                // accumulate coefficient gradients
+    int derived;             // the forward ran the tiled kernels: VW2 = VU2 VW3 c_vw2, S3 = P1 c_s3 (the stored
+                             // VW2 and S3 are not read, their gradients go to VU2, VW3 and P1)
 };
 
 // Tensor maps of the twelve staged arrays of one gather (x windows, y windows, z-ring rows; adjoint.cu), and of

@@ -1050,6 +1050,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemsetAsync(d_gw, 0, (size_t)nt * 8, c->stream));
     CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
     a.grad = 1;
+    a.derived = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? 1 : 0;
     AdjMaps* maps = static_cast<AdjMaps*>(std::aligned_alloc(alignof(AdjMaps), sizeof(AdjMaps)));
     if (!maps) return fail(BEHF_ERR_ALLOC, "host allocation of the adjoint tensor maps");
     std::unique_ptr<AdjMaps, void (*)(void*)> maps_owner(maps, std::free);
