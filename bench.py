@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient (adjoint) measurement")
     ap.add_argument("--adjoint-n", type=int, default=256, help="grid of the gradient measurement")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only the gradient measurement (one JSON object with the adjoint leg)")
     return ap.parse_args()
 
 
@@ -352,6 +354,12 @@ def main():
         return
     import behf
     behf.load()
+    if args.adjoint_only:
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            print(json.dumps({"adjoint": adjoint_leg(args)}), flush=True)
+        return
     behf_arm(args, world, rank, local)
 
 
