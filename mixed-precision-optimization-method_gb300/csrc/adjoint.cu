@@ -940,7 +940,6 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
                   const GatherMaps* snapV, int fuse, cudaStream_t st) {
     const dim3 block(32, 8, 1);
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
-    // gathers: z chunks so that about eight CTAs per SM are launched
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -948,10 +947,9 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
+    // z chunks (2 CTAs per SM resident) that fill the last wave, at most 64 planes
     const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
-    int nch = (8 * sms + nxy - 1) / nxy;
-    nch = std::max(1, std::min(nch, std::max(1, nzu / 8)));
-    const int zc = (nzu + nch - 1) / nch;
+    const int zc = wave_zchunk(nxy, nzu, 2 * sms, 8, 64, R);
     const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);
     StageSet t{}, v{};
     // T^T gather: x {T0 s4, T4 s6h, T5 s7h, T3 s5}, y {T1 s4, T4 s6h, T6 s7h, T3 s5}, z {T2 s4, T5 s6h, T6 s7h, T3 s5}

@@ -609,17 +609,12 @@ template <class S, int R>
 cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) {
     const int nbx = (g.nx - R + TXC - 1) / TXC, nby = (g.ny - R + TY - 1) / TY;
     const int planes = g.nz - 2 * R;
-    // enough CTAs for every SM: split z into chunks when the xy tiling alone is too small
-    const int target = 2 * (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
-    int nzc = (target + nbx * nby - 1) / (nbx * nby);
-    nzc = nzc < 1 ? 1 : nzc;
-    const int maxc = planes / 16 > 1 ? planes / 16 : 1;
-    nzc = nzc > maxc ? maxc : nzc;
-    int zchunk = (planes + nzc - 1) / nzc;
-    // short z ranges keep the CTAs that share halo rows marching the same planes at the same time, so the
-    // rows one CTA brings into L2 are still there when its neighbours read them (measured at 1024^3 FP16:
-    // 64-plane chunks 34.7 ms per step against 40.2 ms for whole columns)
-    if (zchunk > BEHF_TILED_ZCHUNK) zchunk = BEHF_TILED_ZCHUNK;
+    // z chunks of at most BEHF_TILED_ZCHUNK planes: short z ranges keep the CTAs that share halo rows marching the
+    // same planes at the same time, so the rows one CTA brings into L2 are still there when its neighbours read
+    // them (measured at 1024^3 FP16: 64-plane chunks 34.7 ms per step against 40.2 ms for whole columns); within
+    // that, a chunk count that fills the last wave of resident CTAs (MINB per SM)
+    const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
+    int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R);
     if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
