@@ -947,9 +947,10 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    // z chunks (2 CTAs per SM resident) that fill the last wave, at most 64 planes
+    // z chunks (2 CTAs per SM resident) that fill the last wave, at most 64 planes, at least 4 waves (measured at
+    // 192^3: 2 waves of 46-plane chunks 553 + 615 us per step, 5 waves of 17 planes 521 + 522 us)
     const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
-    const int zc = wave_zchunk(nxy, nzu, 2 * sms, 8, 64, R);
+    const int zc = wave_zchunk(nxy, nzu, 2 * sms, 8, 64, R, 4);
     const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);
     StageSet t{}, v{};
     // T^T gather: x {T0 s4, T4 s6h, T5 s7h, T3 s5}, y {T1 s4, T4 s6h, T6 s7h, T3 s5}, z {T2 s4, T5 s6h, T6 s7h, T3 s5}
