@@ -99,6 +99,9 @@ enum {
     BEHF_OPT_STATE_ROUNDING = 7, /* FP16/BF16 kinds, tiled kernels: 0 fields stored rounded to nearest, 1 stochastic
                                     rounding (seeded by step, field and cell), which keeps increments smaller than
                                     half a unit in the last place in expectation instead of dropping them */
+    BEHF_OPT_SNAPSHOT_CACHE = 8, /* gradient: device memory for keeping the forward pass's per-step snapshots of the
+                                    last checkpoint segments, which then need no recompute (-1 = automatic: the free
+                                    memory but max(8 GiB, 10 % of the device); 0 = none; n > 0 = at most n MiB) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current

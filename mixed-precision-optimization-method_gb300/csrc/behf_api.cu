@@ -129,6 +129,7 @@ struct behf_ctx {
     bool keep_medium = false;
     float* d_mod[kNMod] = {};
     int ck_stride = 0;
+    int snap_cache_mib = -1;  // gradient: device memory for snapshots kept from the forward pass (-1 automatic)
     int coef_dither = 0;  // BEHF_OPT_COEF_ROUNDING
 
     ~behf_ctx() {
@@ -843,6 +844,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative checkpoint spacing");
             c->ck_stride = value;
             break;
+        case BEHF_OPT_SNAPSHOT_CACHE:
+            if (value < -1) return fail(BEHF_ERR_INVALID, "snapshot cache must be -1 (automatic), 0 or a size in MiB");
+            c->snap_cache_mib = value;
+            break;
         case BEHF_OPT_COEF_ROUNDING:
             if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "coefficient rounding must be 0 or 1");
             if (c->medium_set) return fail(BEHF_ERR_STATE, "BEHF_OPT_COEF_ROUNDING must be set before the medium");
@@ -1055,18 +1060,49 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     if (!maps) return fail(BEHF_ERR_ALLOC, "host allocation of the adjoint tensor maps");
     std::unique_ptr<AdjMaps, void (*)(void*)> maps_owner(maps, std::free);
     CK(adj_build_maps<S>(g, a, maps));
-    // tensor maps of every snapshot buffer (slot u holds the fields after V of step s0 + u - 1; slot 0 the state
-    // after step s0 - 1, whose velocities and Darcy velocities are those after its V)
+    // Snapshots of a segment: slot u holds the fields after V (+ force) of step s0 + u - 1, slot 0 the state after
+    // step s0 - 1 (its velocities and Darcy velocities are those after its V).  The last segments keep the
+    // snapshots of the forward pass in a cache and need no recompute: as many as the free device memory allows
+    // (BEHF_OPT_SNAPSHOT_CACHE: -1 all of it but max(8 GiB, 10 %), 0 none, else that many MiB); their slot 0 is the
+    // segment's checkpoint, which holds the 13 fields in the same layout.  The others share one buffer.
+    std::vector<char*> cache(nseg, nullptr);
+    if (c->snap_cache_mib != 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const size_t margin = std::max((size_t)8 << 30, tot / 10);
+        size_t budget = fr > margin ? fr - margin : 0;
+        if (c->snap_cache_mib > 0) budget = std::min(budget, (size_t)c->snap_cache_mib << 20);
+        const size_t per = snap_bytes * (size_t)S_;
+        const int ncached = (int)std::min<size_t>((size_t)nseg, budget / per);
+        for (int k = 0; k < ncached; k++)
+            if (buf.get((void**)&cache[nseg - 1 - k], per) != BEHF_OK) {  // keep what fitted
+                cache[nseg - 1 - k] = nullptr;
+                break;
+            }
+    }
+    auto snap_ptr = [&](int sg, int idx, int f) -> char* {
+        const size_t fo = align256(nf * c->es) * f;
+        if (cache[sg]) return idx == 0 ? ck + ck_bytes * sg + fo : cache[sg] + snap_bytes * (idx - 1) + fo;
+        return snap + snap_bytes * idx + fo;
+    };
+    // tensor maps of a segment's snapshot slots (the 16-bit kinds stage snapshot windows in the gathers)
     std::vector<GatherMaps> snap_mt, snap_mv;
-    if (adj_snap_staged<S>()) {
+    int maps_seg = -2;  // segment whose buffers the maps describe (-1: the shared buffer)
+    auto build_snap_maps = [&](int sg) -> cudaError_t {
+        if (!adj_snap_staged<S>()) return cudaSuccess;
+        const int key = cache[sg] ? sg : -1;
+        if (key == maps_seg) return cudaSuccess;
         snap_mt.resize(S_ + 1);
         snap_mv.resize(S_ + 1);
         for (int u = 0; u <= S_; u++) {
             void* f[kNField];
-            for (int q = 0; q < kNField; q++) f[q] = snap + snap_bytes * u + (size_t)q * align256(nf * c->es);
-            CK(adj_build_snap_maps<S>(g, f, &snap_mt[u], &snap_mv[u]));
+            for (int q = 0; q < kNField; q++) f[q] = snap_ptr(sg, u, q);
+            const cudaError_t e = adj_build_snap_maps<S>(g, f, &snap_mt[u], &snap_mv[u]);
+            if (e != cudaSuccess) return e;
         }
-    }
+        maps_seg = key;
+        return cudaSuccess;
+    };
 
     auto copy_state = [&](char* dst, bool save) -> cudaError_t {
         char* q = dst;
@@ -1085,24 +1121,53 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                 }
         return cudaSuccess;
     };
-    auto snap_fields = [&](int idx) -> cudaError_t {
-        char* q = snap + snap_bytes * idx;
-        for (int f = 0; f < kNField; f++, q += align256(nf * c->es)) {
-            cudaError_t e = cudaMemcpyAsync(q, c->p.f[f], nf * c->es, cudaMemcpyDeviceToDevice, c->stream);
+    auto snap_fields = [&](int sg, int idx) -> cudaError_t {
+        for (int f = 0; f < kNField; f++) {
+            cudaError_t e = cudaMemcpyAsync(snap_ptr(sg, idx, f), c->p.f[f], nf * c->es, cudaMemcpyDeviceToDevice,
+                                            c->stream);
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
     };
-    auto snap_ptr = [&](int idx, int f) -> const void* { return snap + snap_bytes * idx + align256(nf * c->es) * f; };
+    double fac = 0;
+    CK(source_factor(c, &fac));
+    const long long so = c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]);
+    // one forward step with the d_it counter, keeping the fields after V (+ force) in slot idx of segment sg
+    auto snap_step = [&](int sg, int idx, bool record) -> cudaError_t {
+        cudaError_t e;
+        if (c->src_kind != BEHF_SRC_FORCE_Z &&
+            (e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
+            return e;
+        if ((e = dispatch_update(c, true)) != cudaSuccess) return e;
+        if (c->src_kind == BEHF_SRC_FORCE_Z &&
+            (e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
+            return e;
+        if ((e = snap_fields(sg, idx)) != cudaSuccess) return e;
+        if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
+        if (record) {
+            RecScales rs;
+            for (int q = 0; q < kNField; q++) rs.s[q] = c->field_scale(q);
+            if ((e = aux_record<S>(c->p, c->d_rec_off, c->d_rec_comp, c->nrec, c->d_seis, c->cap, c->d_it, 0, rs,
+                                   c->stream)) != cudaSuccess)
+                return e;
+        }
+        c->launches += 4 + (record ? 1 : 0);
+        return aux_tick(c->d_it, 1, c->stream);
+    };
 
-    // forward pass with checkpoints (seismograms recorded as in behf_run)
+    // forward pass with checkpoints (seismograms recorded as in behf_run); cached segments step by step
     st = zero_state(c);
     if (st) return st;
     for (int sg = 0; sg < nseg; sg++) {
         const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
         CK(copy_state(ck + ck_bytes * sg, true));
-        st = behf_run_async(c, s1 - s0);
-        if (st) return st;
+        if (!cache[sg]) {
+            st = behf_run_async(c, s1 - s0);
+            if (st) return st;
+        } else {
+            for (int it = s0; it < s1; it++) CK(snap_step(sg, it - s0 + 1, true));
+            c->step += s1 - s0;
+        }
     }
     st = behf_sync(c);
     if (st) return st;
@@ -1134,32 +1199,22 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     for (int q = 0; q < kNField; q++) sc.s[q] = alpha / c->field_scale(q);
     CK(cudaMemcpy(d_adj, adj.data(), adj.size() * 8, cudaMemcpyHostToDevice));
 
-    double fac = 0;
-    CK(source_factor(c, &fac));
-    const long long so = c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]);
     for (int sg = nseg - 1; sg >= 0; sg--) {
         const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
-        CK(copy_state(ck + ck_bytes * sg, false));
-        CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        CK(snap_fields(0));
-        for (int it = s0; it < s1; it++) {  // recompute, keeping the fields after V (+ force)
-            if (c->src_kind != BEHF_SRC_FORCE_Z)
-                CK(aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream));
-            CK(dispatch_update(c, true));
-            if (c->src_kind == BEHF_SRC_FORCE_Z)
-                CK(aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream));
-            CK(snap_fields(it - s0 + 1));
-            CK(dispatch_update(c, false));
-            CK(aux_tick(c->d_it, 1, c->stream));
-            c->launches += 4;
+        if (!cache[sg]) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
+            CK(copy_state(ck + ck_bytes * sg, false));
+            CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            CK(snap_fields(sg, 0));
+            for (int it = s0; it < s1; it++) CK(snap_step(sg, it - s0 + 1, false));
         }
+        CK(build_snap_maps(sg));
         // backward step it: T^T per cell of it is done (the first step: here, after its record^T; later steps: fused
         // into the V^T gather of step it + 1, completed by the record^T of it)
         for (int it = s1 - 1; it >= s0; it--) {
-            for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(it - s0 + 1, f);
-            for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(it - s0, BEHF_QX + d);
-            for (int d = 0; d < 6; d++) a.vq1[d] = snap_ptr(it - s0, BEHF_VX + d);
+            for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(sg, it - s0 + 1, f);
+            for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(sg, it - s0, BEHF_QX + d);
+            for (int d = 0; d < 6; d++) a.vq1[d] = snap_ptr(sg, it - s0, BEHF_VX + d);
             if (it == nt - 1) {
                 CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
                 CK(adj_first<S>(g, c->p, a, c->stream));

@@ -1,7 +1,8 @@
 """Adjoint-state gradient on the GPU (behf_gradient / behf_misfit_gradient through the C ABI), against the
 FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identity and finite differences):
   * FP64: wavelet and moduli gradients within 1e-9 relative L2 of the oracle, every source kind, radius 1/2/4,
-    with and without CPML; dot-product identity within 1e-10; checkpoint spacing changes nothing;
+    with and without CPML; dot-product identity within 1e-10; checkpoint spacing and the snapshot cache change
+    nothing;
   * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
   * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
 from __future__ import annotations
@@ -31,8 +32,9 @@ def rel(a, b):
     return np.linalg.norm((a - b).ravel()) / d if d > 0 else np.linalg.norm(a.ravel())
 
 
-def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto"):
-    s = behf.solver_for(p, precision=precision, kernel=kernel, gradient=True, checkpoint=checkpoint)
+def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto", snapshot_cache=-1):
+    s = behf.solver_for(p, precision=precision, kernel=kernel, gradient=True, checkpoint=checkpoint,
+                        snapshot_cache=snapshot_cache)
     gw, gm = s.gradient(p.nt, adj)
     seis = s.seismograms()
     s.close()
@@ -79,6 +81,19 @@ def test_gradient_checkpoint_spacing(behf_lib):
     _, gw3, gm3 = gpu_gradient(p, adj, "f64", checkpoint=p.nt)
     for a, b in ((gw1, gw2), (gw1, gw3), (gm1, gm2), (gm1, gm3)):
         np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("precision", ["f64", "f16"])
+def test_gradient_snapshot_cache(behf_lib, precision):
+    # every segment recomputed (0), the last two kept from the forward pass (50 MiB of 1.6 MB slots x 13 per
+    # segment at f64), all kept (-1): the same gradient, bit for bit
+    p = small(R=2, L=4)
+    adj = np.random.default_rng(7).standard_normal((len(p.rec_comp), p.nt))
+    ref = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=0)
+    for cache in (50, -1):
+        out = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=cache)
+        for a, b in zip(out, ref):
+            np.testing.assert_array_equal(a, b)
 
 
 @pytest.mark.parametrize("precision,tol", [("f32", 1e-4), ("f16", 5e-2)])
