@@ -254,7 +254,7 @@ struct StageSet {
 };
 
 template <class S, int R>
-struct G25 {
+struct GatherOps {
     typedef typename Traits<S>::C A;
     // The CPML correction v -> v + B (lpsi + v) + lprev of a value already loaded, in two phases: fix_load issues
     // its three loads unconditionally (at slab cell 0 when (x, y, k) is outside the grid or the slab of axis ax;
@@ -348,7 +348,7 @@ template <class S, int R, int KIND>
 __global__ void __launch_bounds__(256, 2)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
              AdjPtrs a, StageSet ss, int zc, int fuse) {
-    typedef G25<S, R> W;
+    typedef GatherOps<S, R> W;
     typedef Adj<S, R> Q;
     typedef GMap<S, R, KIND> M;
     typedef typename W::A A;

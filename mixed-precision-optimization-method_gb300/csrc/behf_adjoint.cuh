@@ -10,7 +10,8 @@
 //   gather: each field's adjoint takes minus the transposed stencils of the derivative adjoints of its
 //      neighbours, each corrected on the fly by the adjoint CPML memory of the neighbour's slab;
 //   per slab cell: the adjoint CPML memory update  L = lpsi + lD;  lpsi = A L;  lprev = A B L;
-// fused into three launches per step (adjoint.cu).
+// in two TMA-pipelined z-marching gathers per step (the second also does T^T per cell of the next backward
+// step), a slab-only memory kernel and the sparse record^T / source^T launches (adjoint.cu).
 #pragma once
 #include <cuda.h>
 
