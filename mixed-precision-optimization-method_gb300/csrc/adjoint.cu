@@ -247,6 +247,14 @@ __global__ void __launch_bounds__(256) k_adj_a(Geom g, DevPtrs p, AdjPtrs a) {
 // from: lD = lD~ + B (lpsi + lD~) + lprev on slab cells, lD~ elsewhere (zero off the updated cells); applied in
 // shared memory after the copies land (x/y windows of tiles that reach a slab, ring planes inside the z slab).
 constexpr int GX = 32, GY = 8;
+// Tuning: CTAs per SM the gathers' launch bounds aim for (registers capped at 65536 / (256 MINB)), and whether the
+// 16-bit kinds stage the forward snapshot for the gradient stencils (1) or read it from global memory (0).
+#ifndef BEHF_ADJ_MINB
+#define BEHF_ADJ_MINB 2
+#endif
+#ifndef BEHF_ADJ_SNAP
+#define BEHF_ADJ_SNAP 1
+#endif
 
 struct StageSet {
     int slot[3][4];  // [axis][array]: adjoint CPML memory slot and half-shift flag of each staged array
@@ -312,7 +320,7 @@ struct GMap {
     static constexpr bool YV = (R * (int)sizeof(A)) % 16 == 0;
     static constexpr int YW = YV ? GX : XWP;
     static constexpr int YC = YV ? 0 : R;
-    static constexpr bool SNAP = sizeof(S) == 2;
+    static constexpr bool SNAP = BEHF_ADJ_SNAP && sizeof(S) == 2;
     static constexpr int CHS = 16 / (int)sizeof(S);
     static constexpr int XWPS = (XW + CHS - 1) / CHS * CHS;
     static constexpr bool YVS = (R * (int)sizeof(S)) % 16 == 0;
@@ -345,7 +353,7 @@ struct GMap {
 // maps.m[0..3]: x windows, [4..7]: y windows, [8..11]: ring rows, in the order above; smaps: the same for the
 // snapshot arrays (SNAP only).
 template <class S, int R, int KIND>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
              AdjPtrs a, StageSet ss, int zc, int fuse) {
     typedef GatherOps<S, R> W;
@@ -1048,7 +1056,7 @@ cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
 }
 template <class S>
 bool adj_snap_staged() {
-    return sizeof(S) == 2;
+    return BEHF_ADJ_SNAP && sizeof(S) == 2;
 }
 template <class S>
 cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv) {
