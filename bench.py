@@ -203,9 +203,9 @@ def timed_steps(s, steps, world):
     ms = e0.elapsed_time(e1)
     launches = s.info()["launches"] - l0
     if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        from behf import replicas
+
+        ms = replicas.max_over_ranks(ms, device="cuda")
     return ms, launches
 
 
