@@ -235,6 +235,12 @@ behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, doubl
  * waits for all.  Equivalent to behf_run on each context in turn. */
 behf_status behf_run_batch(behf_ctx* const* ctxs, int n, int nsteps);
 
+/* Self-test of failure detection (no counterpart in the reference): launches on the context's stream one block
+ * that waits, with the bounded wait of the TMA pipelines (about 2 s), on a barrier that nothing releases, then
+ * syncs.  Returns BEHF_ERR_TIMEOUT, as behf_sync does after a pipeline wait gave up; the context stays usable
+ * (the error word is cleared). */
+behf_status behf_selftest_wait(behf_ctx* ctx);
+
 /* Text of the last error on this thread. */
 const char* behf_last_error(void);
 /* Library version string. */

@@ -118,6 +118,7 @@ def load() -> C.CDLL:
         "behf_misfit_gradient": [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double),
                                  P(P(C.c_double))],
         "behf_autotune": [C.c_void_p, C.c_int, P(C.c_int), P(C.c_double)],
+        "behf_selftest_wait": [C.c_void_p],
         "behf_run_batch": [P(C.c_void_p), C.c_int, C.c_int],
         "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                     C.c_void_p, C.c_void_p, C.c_void_p],
@@ -283,6 +284,11 @@ class Solver:
         z, ms = C.c_int(0), C.c_double(0)
         _check(self._lib.behf_autotune(self._ctx, int(trial_steps), C.byref(z), C.byref(ms)))
         return z.value, ms.value
+
+    def selftest_wait(self) -> int:
+        """Failure-detection self-test: a bounded pipeline wait that nothing releases (about 2 s); returns the
+        status code, BEHF_ERR_TIMEOUT (-7) when detection works.  The context stays usable."""
+        return int(self._lib.behf_selftest_wait(self._ctx))
 
     # -- gradient (adjoint state, checkpointed)
     def enable_gradient(self, checkpoint: int = 0, snapshot_cache: int = -1):

@@ -1334,6 +1334,13 @@ behf_status behf_misfit_gradient(behf_ctx* c, int nt, const double* observed, do
     return gradient_dispatch(c, nt, nullptr, observed, misfit, grad_wavelet, grad_moduli);
 }
 
+behf_status behf_selftest_wait(behf_ctx* c) {
+    if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    CK(aux_wait_selftest(c->d_err, c->stream));
+    c->launches++;
+    return behf_sync(c);
+}
+
 behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double* ms_out) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
     if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_autotune");

@@ -32,6 +32,7 @@ template <class S>
 cudaError_t aux_record(const DevPtrs& p, const long long* off, const int* comp, int nrec, double* seis, int cap,
                        const int* d_it, int s_off, const RecScales& sc, cudaStream_t st);
 cudaError_t aux_tick(int* d_it, int n, cudaStream_t st);
+cudaError_t aux_wait_selftest(int* err, cudaStream_t st);
 template <class S>
 cudaError_t aux_health(const void* f, int nx, int ny, int nz, long long px, long long plane, double limit,
                        double* part, int nblk, int* flag, double* out, cudaStream_t st);

@@ -11,6 +11,7 @@
 #include <cfloat>
 
 #include "behf_aux.cuh"
+#include "kernels_tiled.cuh"
 
 namespace behf {
 
@@ -303,6 +304,24 @@ cudaError_t aux_record(const DevPtrs& p, const long long* off, const int* comp, 
 
 cudaError_t aux_tick(int* d_it, int n, cudaStream_t st) {
     k_tick<<<1, 1, 0, st>>>(d_it, n);
+    return cudaGetLastError();
+}
+
+// Self-test of the pipelines' bounded wait: every thread waits (tiled::mbar_wait, the wait of the TMA pipelines)
+// on an mbarrier that nothing arrives at; the wait gives up after its cycle limit and the block reports through
+// the context's error word, exactly as a pipeline kernel whose copies never land.
+__global__ void k_wait_selftest(int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tiled::mbar_init(&bar, 1);
+        tiled::fence_init();
+    }
+    __syncthreads();
+    const bool ok = tiled::mbar_wait(&bar, 0u);
+    if (!__all_sync(0xffffffffu, ok) && threadIdx.x == 0) atomicExch(err, 1);
+}
+cudaError_t aux_wait_selftest(int* err, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(err);
     return cudaGetLastError();
 }
 

@@ -188,6 +188,22 @@ def test_errors_are_reported_not_fatal(behf_lib):
     s.close()
 
 
+def test_bounded_wait_timeout_is_reported(behf_lib, oracle):
+    # failure detection without a GPU fault: a pipeline wait that nothing releases gives up (about 2 s), the
+    # status is BEHF_ERR_TIMEOUT, and the context still runs correctly afterwards
+    import behf
+    p = _problem(n=24, nt=60, radius=2)
+    s = behf.solver_for(p, precision="f32", kernel="tiled")
+    assert s.selftest_wait() == -7
+    assert "timed out" in behf.load().behf_last_error().decode()
+    s.run(p.nt)
+    seis = s.seismograms()
+    s.close()
+    ref, _ = oracle.run(p, "f64")
+    errs = _per_field_err(oracle, p, seis, ref)
+    assert max(errs.values()) < TOL["f32"], errs
+
+
 def _odd_problem(shape, radius, nt, cpml=5):
     from behf import problems
     nx, ny, nz = shape
