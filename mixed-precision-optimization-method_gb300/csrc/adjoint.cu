@@ -255,6 +255,18 @@ constexpr int GX = 32, GY = 8;
 #ifndef BEHF_ADJ_SNAP
 #define BEHF_ADJ_SNAP 1
 #endif
+// 1: the coefficient gradients run in kernels of their own (MODE 2) after register-lean gathers (MODE 1), at
+// BEHF_ADJ_MINB_SPLIT CTAs per SM; 0: fused into the gathers (MODE 0).
+#ifndef BEHF_ADJ_SPLIT
+#define BEHF_ADJ_SPLIT 1
+#endif
+#ifndef BEHF_ADJ_MINB_SPLIT
+#define BEHF_ADJ_MINB_SPLIT 3
+#endif
+// the split V^T gather (T-slot memory and T^T per cell of the next step): its CTAs per SM
+#ifndef BEHF_ADJ_MINB_G1
+#define BEHF_ADJ_MINB_G1 2
+#endif
 
 struct StageSet {
     int slot[3][4];  // [axis][array]: adjoint CPML memory slot and half-shift flag of each staged array
@@ -309,10 +321,13 @@ struct GatherOps {
 // holds [4 x][4 y] windows of forward snapshot fields (type S) and a second ring holds their z rows, for the
 // stencils of the coefficient gradients: KIND 0 stresses and pressure of step n (x: sxx sxy sxz p, y: syy sxy
 // syz p, z: szz sxz syz p), KIND 1 velocities and Darcy velocities of step n - 1 (x: vx vy vz qx, y: vy vx vz qy,
-// z: vz vx vy qz).  Every box starts on a 128-byte boundary.
-template <class S, int R, int KIND>
+// z: vz vx vy qz).  MODE 0: adjoint windows and, for the 16-bit kinds, the snapshot (gather and gradients fused);
+// MODE 1: adjoint windows only (the gather); MODE 2: the snapshot only (the gradients).  Every box starts on a
+// 128-byte boundary.
+template <class S, int R, int MODE>
 struct GMap {
     typedef typename Traits<S>::C A;
+    static constexpr bool TMP = MODE != 2;
     static constexpr int XW = GX + 2 * R;
     static constexpr int YH = GY + 2 * R;
     static constexpr int CH = 16 / (int)sizeof(A);
@@ -320,7 +335,7 @@ struct GMap {
     static constexpr bool YV = (R * (int)sizeof(A)) % 16 == 0;
     static constexpr int YW = YV ? GX : XWP;
     static constexpr int YC = YV ? 0 : R;
-    static constexpr bool SNAP = BEHF_ADJ_SNAP && sizeof(S) == 2;
+    static constexpr bool SNAP = MODE == 2 || (MODE == 0 && BEHF_ADJ_SNAP && sizeof(S) == 2);
     static constexpr int CHS = 16 / (int)sizeof(S);
     static constexpr int XWPS = (XW + CHS - 1) / CHS * CHS;
     static constexpr bool YVS = (R * (int)sizeof(S)) % 16 == 0;
@@ -328,9 +343,9 @@ struct GMap {
     static constexpr int YCS = YVS ? 0 : R;
     static constexpr int ZS = 2 * R + 2;
     static constexpr int NS = 2;
-    static constexpr int XBOX = tiled::al128(XWP * GY * (int)sizeof(A));
-    static constexpr int YBOX = tiled::al128(YW * YH * (int)sizeof(A));
-    static constexpr int ZBOX = tiled::al128(YW * GY * (int)sizeof(A));
+    static constexpr int XBOX = TMP ? tiled::al128(XWP * GY * (int)sizeof(A)) : 0;
+    static constexpr int YBOX = TMP ? tiled::al128(YW * YH * (int)sizeof(A)) : 0;
+    static constexpr int ZBOX = TMP ? tiled::al128(YW * GY * (int)sizeof(A)) : 0;
     static constexpr int XBOXS = SNAP ? tiled::al128(XWPS * GY * (int)sizeof(S)) : 0;
     static constexpr int YBOXS = SNAP ? tiled::al128(YWS * YH * (int)sizeof(S)) : 0;
     static constexpr int ZBOXS = SNAP ? tiled::al128(YWS * GY * (int)sizeof(S)) : 0;
@@ -339,8 +354,8 @@ struct GMap {
     static constexpr int RING = NS * STAGE;
     static constexpr int RINGS = RING + 4 * ZS * ZBOX;
     static constexpr int BYTES = RINGS + 4 * ZS * ZBOXS;
-    static constexpr uint32_t STAGE_TX = 4u * (XWP * GY + YW * YH) * (uint32_t)sizeof(A);
-    static constexpr uint32_t Z_TX = 4u * YW * GY * (uint32_t)sizeof(A);
+    static constexpr uint32_t STAGE_TX = TMP ? 4u * (XWP * GY + YW * YH) * (uint32_t)sizeof(A) : 0u;
+    static constexpr uint32_t Z_TX = TMP ? 4u * YW * GY * (uint32_t)sizeof(A) : 0u;
     static constexpr uint32_t STAGE_TXS = SNAP ? 4u * (XWPS * GY + YWS * YH) * (uint32_t)sizeof(S) : 0u;
     static constexpr uint32_t Z_TXS = SNAP ? 4u * YWS * GY * (uint32_t)sizeof(S) : 0u;
 };
@@ -350,15 +365,20 @@ struct GMap {
 // KIND 1: V^T gather (X: V0 s0h, V1 s2, V2 s3, V3 s1h;  Y: V1 s0h, V0 s2, V2 s3, V4 s1h;
 //                      Z: V2 s0h, V0 s2, V1 s3, V5 s1h), then the T-slot memory update and, with fuse, T^T per
 //                      cell of step n - 1.
+// MODE 1 (split gathers): KIND 0 stores mu = lq' - VU2 lv' of the cells outside the slabs for the gradient
+// kernel; KIND 1 does T^T per cell without its gradient.  MODE 2 (gradients, after the gather of the same KIND):
+// KIND 0 the V-coefficient gradients of step n from mu, lv and the staged stresses and pressure; KIND 1 the
+// T-coefficient gradients of step n - 1 from the new stress and pressure adjoints and the staged velocities.
 // maps.m[0..3]: x windows, [4..7]: y windows, [8..11]: ring rows, in the order above; smaps: the same for the
 // snapshot arrays (SNAP only).
-template <class S, int R, int KIND>
-__global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
+template <class S, int R, int KIND, int MODE>
+__global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
+                                       : (MODE == 1 && KIND == 1) ? BEHF_ADJ_MINB_G1 : BEHF_ADJ_MINB_SPLIT)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
              AdjPtrs a, StageSet ss, int zc, int fuse) {
     typedef GatherOps<S, R> W;
     typedef Adj<S, R> Q;
-    typedef GMap<S, R, KIND> M;
+    typedef GMap<S, R, MODE> M;
     typedef typename W::A A;
     using namespace tiled;
     extern __shared__ __align__(128) unsigned char gsm_raw[];
@@ -385,9 +405,10 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
     auto has_int = [&](int lo, int hi, int n) { return g.W == 0 || max(lo, g.L) <= min(hi, n - 2 - g.L); };
     const bool snap = M::SNAP && a.grad && (KIND == 0 || fuse) && has_int(i0, i0 + GX - 1, g.nx) &&
                       has_int(j0, j0 + GY - 1, g.ny) && has_int(kb, ke - 1, g.nz);
+    if (MODE == 2 && !snap) return;  // a gradient CTA without cells outside the slabs has nothing to do
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
-    const bool cx = g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
-    const bool cy = g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
+    const bool cx = M::TMP && g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
+    const bool cy = M::TMP && g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
     const bool fixcta = cx || cy;
 
     if (tid == 0) {
@@ -404,13 +425,15 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
         uint64_t* br = &bfull[st];
         const uint32_t nz_ = warm ? 2 * R + 1 : 1;
         mbar_expect_tx(br, M::STAGE_TX + M::Z_TX * nz_ + (snap ? M::STAGE_TXS + M::Z_TXS * nz_ : 0u));
+        if (M::TMP) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) tma3(X(st, q), &maps.m[q], br, i0 - R, j0, kk);
+            for (int q = 0; q < 4; q++) tma3(X(st, q), &maps.m[q], br, i0 - R, j0, kk);
 #pragma unroll
-        for (int q = 0; q < 4; q++) tma3(Y(st, q), &maps.m[4 + q], br, yx0, j0 - R, kk);
-        for (int z = warm ? kk - R : kk + R; z <= kk + R; z++)
+            for (int q = 0; q < 4; q++) tma3(Y(st, q), &maps.m[4 + q], br, yx0, j0 - R, kk);
+            for (int z = warm ? kk - R : kk + R; z <= kk + R; z++)
 #pragma unroll
-            for (int q = 0; q < 4; q++) tma3(Z(q, z % M::ZS), &maps.m[8 + q], br, yx0, j0, z);
+                for (int q = 0; q < 4; q++) tma3(Z(q, z % M::ZS), &maps.m[8 + q], br, yx0, j0, z);
+        }
         if (snap) {
 #pragma unroll
             for (int q = 0; q < 4; q++) tma3(XS(st, q), &smaps.m[q], br, i0 - R, j0, kk);
@@ -452,7 +475,7 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
         fph ^= 1u << st;
         if (tid == 0) pend &= ~(1u << st);
         // ring planes that arrived with this stage and lie in the z slab: each thread corrects its own column
-        if (g.W > 0 && valid) {
+        if (M::TMP && g.W > 0 && valid) {
             for (int z = it == 0 ? k - R : k + R; z <= k + R; z++) {
                 if (slab_index(z, g.nz, g.L) < 0) continue;
                 typename W::Fix f[4];
@@ -506,15 +529,17 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
         }
         if (valid) {
             const long long c = k * sz + j * sy + i;
-            // element offsets: array q of the x (y) windows at q * XE (q * YE) from the first, ring row of array q
-            // and plane k + d at q * ZS * ZE + zoff[d + R]
+            const bool inner = interior(g, i, j, k);
+            // adjoint windows (M::TMP): array q of the x (y) windows at q * XE (q * YE) from the first; the ring
+            // row of array q and plane k + d at q * ZS * ZE + zoff[d + R]
             constexpr int XE = M::XBOX / (int)sizeof(A), YE = M::YBOX / (int)sizeof(A), ZE = M::ZBOX / (int)sizeof(A);
             const A* xb = X(st, 0) + ty * M::XWP + tx + R;
             const A* yb = Y(st, 0) + (ty + R) * M::YW + M::YC + tx;
             const A* zb = Z(0, 0) + ty * M::YW + M::YC + tx;
+            const int zs0 = (k - R) % M::ZS;  // ring slot of plane k - R
             int zoff[2 * R + 1];
             {
-                int s0 = (k - R) % M::ZS;
+                int s0 = zs0;
 #pragma unroll
                 for (int d = 0; d <= 2 * R; d++) {
                     zoff[d] = s0 * ZE;
@@ -524,8 +549,128 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
 #define WX(q) [&](int d) { return xb[(q) * XE + d]; }
 #define WY(q) [&](int d) { return yb[(q) * YE + d * M::YW]; }
 #define WZ(q) [&](int d) { return zb[(q) * M::ZS * ZE + zoff[R + d]]; }
+            // snapshot windows (M::SNAP), the same arrangement in the storage type
+            constexpr int XES = M::XBOXS / (int)sizeof(S), YES = M::YBOXS / (int)sizeof(S);
+            constexpr int ZES = M::ZBOXS / (int)sizeof(S);
+            const S* xs = XS(st, 0) + ty * M::XWPS + tx + R;
+            const S* ys = YS(st, 0) + (ty + R) * M::YWS + M::YCS + tx;
+            const S* zsb = ZS_(0, 0) + ty * M::YWS + M::YCS + tx;
+            auto zsl = [&](int d) { return zs0 + R + d >= M::ZS ? zs0 + R + d - M::ZS : zs0 + R + d; };
+#define SXW(q) [&](int d) { return Q::ls(xs, (q) * XES + d); }
+#define SYW(q) [&](int d) { return Q::ls(ys, (q) * YES + d * M::YWS); }
+#define SZW(q) [&](int d) { return Q::ls(zsb, ((q) * M::ZS + zsl(d)) * ZES); }
+            // stress divergences and pressure gradient of the forward snapshot of step n (KIND 0)
+            auto t_stencils = [&](A (&sum)[3], A (&dp)[3]) {
+                if constexpr (M::SNAP) {  // x: sxx sxy sxz p;  y: syy sxy syz p;  z: szz sxz syz p
+                    sum[0] = W::fwd(SXW(0)) + W::bwd(SYW(1)) + W::bwd(SZW(1));
+                    sum[1] = W::fwd(SYW(0)) + W::bwd(SXW(1)) + W::bwd(SZW(2));
+                    sum[2] = W::fwd(SZW(0)) + W::bwd(SXW(2)) + W::bwd(SYW(2));
+                    dp[0] = W::fwd(SXW(3));
+                    dp[1] = W::fwd(SYW(3));
+                    dp[2] = W::fwd(SZW(3));
+                } else {
+                    sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) +
+                             Q::bwd(a.cur[BEHF_SXZ], c, sz);
+                    sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) +
+                             Q::bwd(a.cur[BEHF_SYZ], c, sz);
+                    sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) +
+                             Q::bwd(a.cur[BEHF_SYZ], c, sy);
+                    dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
+                    dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
+                    dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
+                }
+            };
+            // velocity and Darcy-velocity derivatives of the forward snapshot of step n - 1 (KIND 1)
+            auto v_stencils = [&](A (&du)[10]) {
+                if constexpr (M::SNAP) {  // x: vx vy vz qx;  y: vy vx vz qy;  z: vz vx vy qz
+                    du[0] = W::bwd(SXW(0));                                    // uxx
+                    du[1] = W::bwd(SYW(0));                                    // uyy
+                    du[2] = W::bwd(SZW(0));                                    // uzz
+                    du[3] = W::bwd(SXW(3)) + W::bwd(SYW(3)) + W::bwd(SZW(3));  // div q
+                    du[4] = W::fwd(SYW(1));                                    // uxy
+                    du[5] = W::fwd(SXW(1));                                    // uyx
+                    du[6] = W::fwd(SZW(1));                                    // uxz
+                    du[7] = W::fwd(SXW(2));                                    // uzx
+                    du[8] = W::fwd(SZW(2));                                    // uyz
+                    du[9] = W::fwd(SYW(2));                                    // uzy
+                } else {
+                    vq_derivs<S, R>(a.vq1, c, sy, sz, du);
+                }
+            };
+            // V-coefficient gradient increments of step n into go (accumulators 0..14) from mu, lv and the
+            // snapshot's q before and after V, stress divergences and pressure gradient
+            auto v_grad = [&](A (&go)[15], const A (&mu)[3], const A (&lv)[3], const A (&qo)[3], const A (&qn)[3],
+                              const A (&sum)[3], const A (&dp)[3], const A (&vu2)[3], const A (&vw3)[3]) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    go[VW1X + d] += mu[d] * qo[d];
+                    const A gw2 = -mu[d] * sum[d];
+                    if (a.derived) {  // chain rule through VW2 = VU2 VW3 c_vw2
+                        go[VU2X + d] += gw2 * vw3[d] * (A)g.c_vw2;
+                        go[VW3X + d] += gw2 * vu2[d] * (A)g.c_vw2;
+                    } else {
+                        go[VW2X + d] += gw2;
+                    }
+                    go[VU1X + d] += lv[d] * sum[d];
+                    go[VU2X + d] += -lv[d] * (qn[d] - qo[d]);
+                }
+                go[VW3X] += -mu[0] * dp[0];
+                const A w3z = -mu[2] * dp[2];
+                go[VW3Y] += -mu[1] * dp[1] + (g.bug ? w3z : (A)0);
+                go[VW3Z] += g.bug ? (A)0 : w3z;
+            };
+            auto load_vgo = [&](A (&go)[15]) {
+#pragma unroll
+                for (int q = 0; q < 15; q++)
+                    go[q] = (a.derived && q >= VW2X && q <= VW2Z) ? (A)0 : Q::ad(a.g[q])[c];
+            };
+            auto store_vgo = [&](const A (&go)[15]) {
+#pragma unroll
+                for (int q = 0; q < 15; q++)
+                    if (!(a.derived && q >= VW2X && q <= VW2Z)) Q::ad(a.g[q])[c] = go[q];
+            };
+            auto load_tgo = [&](A (&go)[8]) {
+#pragma unroll
+                for (int q = 0; q < 8; q++) go[q] = (q == 4 && a.derived) ? (A)0 : Q::ad(a.g[P1 + q])[c];
+            };
+            auto store_tgo = [&](const A (&lt)[7], const A (&du)[10], const A (&go)[8]) {
+                A inc[8];
+                t_grad(lt, du, inc);
+                t_grad_fold(g, a, inc);
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    if (q != 4 || !a.derived) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
+            };
             // Each cell issues all its global loads before its first global store (see k_adj_a).
-            if (KIND == 0) {
+            if constexpr (MODE == 2) {
+                if constexpr (KIND == 0) {  // V-coefficient gradients of step n
+                    if (a.grad && inner) {
+                        A mu[3], lv[3], qo[3], qn[3], vu2[3], vw3[3], go[15], sum[3], dp[3];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            mu[d] = Q::ad(a.mu[d])[c];
+                            lv[d] = Q::ad(a.lf[BEHF_VX + d])[c];
+                            qo[d] = Q::ls(a.qprev[d], c);
+                            qn[d] = Q::ls(a.cur[BEHF_QX + d], c);
+                            vu2[d] = a.derived ? Q::coef(g, p, VU2X + d, c) : (A)0;
+                            vw3[d] = a.derived ? Q::coef(g, p, VW3X + d, c) : (A)0;
+                        }
+                        load_vgo(go);
+                        t_stencils(sum, dp);
+                        v_grad(go, mu, lv, qo, qn, sum, dp, vu2, vw3);
+                        store_vgo(go);
+                    }
+                } else {  // T-coefficient gradients of step n - 1 (the stress/pressure adjoints the gather left)
+                    if (fuse && a.grad && inner) {
+                        A lt[7], go[8], du[10];
+#pragma unroll
+                        for (int q = 0; q < 7; q++) lt[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
+                        load_tgo(go);
+                        v_stencils(du);
+                        store_tgo(lt, du, go);
+                    }
+                }
+            } else if constexpr (KIND == 0) {
                 // V^T at this cell with lv = lv_old - dl[0..2], lq' = lq_old - dl[3..5]
                 A lvo[3], lqo[3], vu2[3], vw1[3], vu1[3], vw2[3], vw3[3], vw3p;
 #pragma unroll
@@ -540,49 +685,16 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
                     vw2[d] = a.derived ? vu2[d] * vw3[d] * (A)g.c_vw2 : Q::coef(g, p, VW2X + d, c);
                 }
                 vw3p = g.bug ? Q::coef(g, p, VW3Y, c) : vw3[2];  // reference: the dp term of vz uses VW3y
-                const bool gr = a.grad && interior(g, i, j, k);
+                const bool gr = a.grad && inner;
                 A sum[3], dp[3], qo[3], qn[3], go[15];
-                if (gr) {
-                    if constexpr (M::SNAP) {  // snapshot stencils from the staged windows (gr implies snap)
-                        constexpr int XES = M::XBOXS / (int)sizeof(S), YES = M::YBOXS / (int)sizeof(S);
-                        constexpr int ZES = M::ZBOXS / (int)sizeof(S);
-                        const S* xs = XS(st, 0) + ty * M::XWPS + tx + R;
-                        const S* ys = YS(st, 0) + (ty + R) * M::YWS + M::YCS + tx;
-                        const S* zsb = ZS_(0, 0) + ty * M::YWS + M::YCS + tx;
-                        const int zs0 = (k - R) % M::ZS;
-                        auto zsl = [&](int d) { return zs0 + R + d >= M::ZS ? zs0 + R + d - M::ZS : zs0 + R + d; };
-#define SXW(q) [&](int d) { return Q::ls(xs, (q) * XES + d); }
-#define SYW(q) [&](int d) { return Q::ls(ys, (q) * YES + d * M::YWS); }
-#define SZW(q) [&](int d) { return Q::ls(zsb, ((q) * M::ZS + zsl(d)) * ZES); }
-                        // x: sxx sxy sxz p;  y: syy sxy syz p;  z: szz sxz syz p
-                        sum[0] = W::fwd(SXW(0)) + W::bwd(SYW(1)) + W::bwd(SZW(1));
-                        sum[1] = W::fwd(SYW(0)) + W::bwd(SXW(1)) + W::bwd(SZW(2));
-                        sum[2] = W::fwd(SZW(0)) + W::bwd(SXW(2)) + W::bwd(SYW(2));
-                        dp[0] = W::fwd(SXW(3));
-                        dp[1] = W::fwd(SYW(3));
-                        dp[2] = W::fwd(SZW(3));
-#undef SXW
-#undef SYW
-#undef SZW
-                    } else {
-                        sum[0] = Q::fwd(a.cur[BEHF_SXX], c, 1) + Q::bwd(a.cur[BEHF_SXY], c, sy) +
-                                 Q::bwd(a.cur[BEHF_SXZ], c, sz);
-                        sum[1] = Q::fwd(a.cur[BEHF_SYY], c, sy) + Q::bwd(a.cur[BEHF_SXY], c, 1) +
-                                 Q::bwd(a.cur[BEHF_SYZ], c, sz);
-                        sum[2] = Q::fwd(a.cur[BEHF_SZZ], c, sz) + Q::bwd(a.cur[BEHF_SXZ], c, 1) +
-                                 Q::bwd(a.cur[BEHF_SYZ], c, sy);
-                        dp[0] = Q::fwd(a.cur[BEHF_P], c, 1);
-                        dp[1] = Q::fwd(a.cur[BEHF_P], c, sy);
-                        dp[2] = Q::fwd(a.cur[BEHF_P], c, sz);
-                    }
+                if (MODE == 0 && gr) {
+                    t_stencils(sum, dp);
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         qo[d] = Q::ls(a.qprev[d], c);
                         qn[d] = Q::ls(a.cur[BEHF_QX + d], c);
                     }
-#pragma unroll
-                    for (int q = 0; q < 15; q++)
-                        go[q] = (a.derived && q >= VW2X && q <= VW2Z) ? (A)0 : Q::ad(a.g[q])[c];
+                    load_vgo(go);
                 }
                 A dl[6];
                 dl[0] = W::fwd(WX(0)) + W::bwd(WY(1)) + W::bwd(WZ(1));
@@ -602,34 +714,20 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
                     Q::ad(a.tmpV[d])[c] = vu1[d] * lv[d] - vw2[d] * mu[d];
                     Q::ad(a.tmpV[3 + d])[c] = -(d == 2 ? vw3p : vw3[d]) * mu[d];
                 }
-                if (gr) {
+                if (MODE == 0 && gr) {
+                    v_grad(go, mu, lv, qo, qn, sum, dp, vu2, vw3);
+                    store_vgo(go);
+                }
+                if (MODE == 1 && gr) {  // for the gradient kernel of this step
 #pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        go[VW1X + d] += mu[d] * qo[d];
-                        const A gw2 = -mu[d] * sum[d];
-                        if (a.derived) {  // chain rule through VW2 = VU2 VW3 c_vw2
-                            go[VU2X + d] += gw2 * vw3[d] * (A)g.c_vw2;
-                            go[VW3X + d] += gw2 * vu2[d] * (A)g.c_vw2;
-                        } else {
-                            go[VW2X + d] += gw2;
-                        }
-                        go[VU1X + d] += lv[d] * sum[d];
-                        go[VU2X + d] += -lv[d] * (qn[d] - qo[d]);
-                    }
-                    go[VW3X] += -mu[0] * dp[0];
-                    const A w3z = -mu[2] * dp[2];
-                    go[VW3Y] += -mu[1] * dp[1] + (g.bug ? w3z : (A)0);
-                    go[VW3Z] += g.bug ? (A)0 : w3z;
-#pragma unroll
-                    for (int q = 0; q < 15; q++)
-                        if (!(a.derived && q >= VW2X && q <= VW2Z)) Q::ad(a.g[q])[c] = go[q];
+                    for (int d = 0; d < 3; d++) Q::ad(a.mu[d])[c] = mu[d];
                 }
             } else {
                 A lo[7];  // sxx syy szz sxy sxz syz p
 #pragma unroll
                 for (int q = 0; q < 7; q++) lo[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
                 // T-slot adjoint memory of this step on slab cells (its gathers ran in the KIND 0 launch)
-                const bool mem = !interior(g, i, j, k);
+                const bool mem = !inner;
                 A tt[7];
                 MemUpd<A, 4, 0xC> mt;
                 if (mem) {
@@ -637,43 +735,15 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
                     for (int q = 0; q < 7; q++) tt[q] = Q::ad(a.tmpT[q])[c];
                     mt.load(g, p, a, i, j, k);
                 }
-                // T^T per cell of step n - 1 (fuse): coefficients, and on cells outside the slabs the forward
-                // derivatives of step n - 1 and the gradient accumulators
+                // T^T per cell of step n - 1 (fuse): coefficients, and (fused gradients) on cells outside the
+                // slabs the forward derivatives of step n - 1 and the gradient accumulators
                 A kc[8];
                 if (fuse) t_coefs<S, R>(g, p, a, c, kc);
-                const bool gr = fuse && a.grad && !mem;
+                const bool gr = MODE == 0 && fuse && a.grad && !mem;
                 A du[10], go[8];
                 if (gr) {
-                    if constexpr (M::SNAP) {  // from the staged windows (gr implies snap)
-                        constexpr int XES = M::XBOXS / (int)sizeof(S), YES = M::YBOXS / (int)sizeof(S);
-                        constexpr int ZES = M::ZBOXS / (int)sizeof(S);
-                        const S* xs = XS(st, 0) + ty * M::XWPS + tx + R;
-                        const S* ys = YS(st, 0) + (ty + R) * M::YWS + M::YCS + tx;
-                        const S* zsb = ZS_(0, 0) + ty * M::YWS + M::YCS + tx;
-                        const int zs0 = (k - R) % M::ZS;
-                        auto zsl = [&](int d) { return zs0 + R + d >= M::ZS ? zs0 + R + d - M::ZS : zs0 + R + d; };
-#define SXW(q) [&](int d) { return Q::ls(xs, (q) * XES + d); }
-#define SYW(q) [&](int d) { return Q::ls(ys, (q) * YES + d * M::YWS); }
-#define SZW(q) [&](int d) { return Q::ls(zsb, ((q) * M::ZS + zsl(d)) * ZES); }
-                        // x: vx vy vz qx;  y: vy vx vz qy;  z: vz vx vy qz
-                        du[0] = W::bwd(SXW(0));                                   // uxx
-                        du[1] = W::bwd(SYW(0));                                   // uyy
-                        du[2] = W::bwd(SZW(0));                                   // uzz
-                        du[3] = W::bwd(SXW(3)) + W::bwd(SYW(3)) + W::bwd(SZW(3));  // div q
-                        du[4] = W::fwd(SYW(1));                                   // uxy
-                        du[5] = W::fwd(SXW(1));                                   // uyx
-                        du[6] = W::fwd(SZW(1));                                   // uxz
-                        du[7] = W::fwd(SXW(2));                                   // uzx
-                        du[8] = W::fwd(SZW(2));                                   // uyz
-                        du[9] = W::fwd(SYW(2));                                   // uzy
-#undef SXW
-#undef SYW
-#undef SZW
-                    } else {
-                        vq_derivs<S, R>(a.vq1, c, sy, sz, du);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 8; q++) go[q] = (q == 4 && a.derived) ? (A)0 : Q::ad(a.g[P1 + q])[c];
+                    v_stencils(du);
+                    load_tgo(go);
                 }
                 A lt[7];
                 lt[0] = lo[0] - W::bwd(WX(0));
@@ -697,15 +767,11 @@ __global__ void __launch_bounds__(256, BEHF_ADJ_MINB)
 #pragma unroll
                     for (int q = 0; q < 7; q++) Q::ad(a.tmpT[q])[c] = tg[q];
                 }
-                if (gr) {
-                    A inc[8];
-                    t_grad(lt, du, inc);
-                    t_grad_fold(g, a, inc);
-#pragma unroll
-                    for (int q = 0; q < 8; q++)
-                        if (q != 4 || !a.derived) Q::ad(a.g[P1 + q])[c] = go[q] + inc[q];
-                }
+                if (gr) store_tgo(lt, du, go);
             }
+#undef SXW
+#undef SYW
+#undef SZW
 #undef WX
 #undef WY
 #undef WZ
@@ -972,18 +1038,28 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
             v.slot[ax][q] = vs[q];
             v.half[ax][q] = vh[q];
         }
-    const int smem0 = GMap<S, R, 0>::BYTES + 128, smem1 = GMap<S, R, 1>::BYTES + 128;
+    constexpr bool split = BEHF_ADJ_SPLIT != 0;
+    constexpr int MG = split ? 1 : 0;  // the gathers' mode
+    const int smemg = GMap<S, R, MG>::BYTES + 128, smemd = GMap<S, R, 2>::BYTES + 128;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem0);
+        cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_gather<S, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1);
+            e = cudaFuncSetAttribute(k_gather<S, R, 1, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);
+        if (e == cudaSuccess && split)
+            e = cudaFuncSetAttribute(k_gather<S, R, 0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemd);
+        if (e == cudaSuccess && split)
+            e = cudaFuncSetAttribute(k_gather<S, R, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemd);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    if (GMap<S, R, 0>::SNAP && a.grad && (!snapT || (fuse && !snapV))) return cudaErrorInvalidValue;
-    k_gather<S, R, 0><<<ggrid, block, smem0, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0);
-    k_gather<S, R, 1><<<ggrid, block, smem1, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse);
+    if ((split || GMap<S, R, 0>::SNAP) && a.grad && (!snapT || (fuse && !snapV))) return cudaErrorInvalidValue;
+    // T^T gather + V^T; its V-coefficient gradients; V^T gather + T-slot memory + T^T of step n - 1; its
+    // T-coefficient gradients
+    k_gather<S, R, 0, MG><<<ggrid, block, smemg, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0);
+    if (split && a.grad) k_gather<S, R, 0, 2><<<ggrid, block, smemd, st>>>(m.t, *snapT, g, p, a, t, zc, 0);
+    k_gather<S, R, 1, MG><<<ggrid, block, smemg, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse);
+    if (split && a.grad && fuse) k_gather<S, R, 1, 2><<<ggrid, block, smemd, st>>>(m.v, *snapV, g, p, a, v, zc, fuse);
     if (g.W > 0) {
         static int sms = 0;
         if (sms == 0) {
@@ -1019,7 +1095,7 @@ cudaError_t build_maps_r(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
     void* const vy_[4] = {a.tmpV[1], a.tmpV[0], a.tmpV[2], a.tmpV[4]};
     void* const vz_[4] = {a.tmpV[2], a.tmpV[0], a.tmpV[1], a.tmpV[5]};
     if (!tiled::encoder()) return cudaErrorNotSupported;
-    typedef GMap<S, R, 0> M;
+    typedef GMap<S, R, 1> M;  // the adjoint-window boxes (the same in the fused mode)
     typedef typename M::A A;
     const bool ok = build_gather_maps<A, M::XWP, M::YW, M::YH>(g, tx_, ty_, tz_, &m->t) &&
                     build_gather_maps<A, M::XWP, M::YW, M::YH>(g, vx_, vy_, vz_, &m->v);
@@ -1028,8 +1104,8 @@ cudaError_t build_maps_r(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
 
 template <class S, int R>
 cudaError_t build_snap_maps_r(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv) {
-    typedef GMap<S, R, 0> M;
-    if (!M::SNAP) return cudaSuccess;
+    typedef GMap<S, R, 2> M;  // the snapshot boxes (the same in the fused mode)
+    if (!BEHF_ADJ_SPLIT && !GMap<S, R, 0>::SNAP) return cudaSuccess;
     if (!tiled::encoder()) return cudaErrorNotSupported;
     void* const x[4] = {f[BEHF_SXX], f[BEHF_SXY], f[BEHF_SXZ], f[BEHF_P]};
     void* const y[4] = {f[BEHF_SYY], f[BEHF_SXY], f[BEHF_SYZ], f[BEHF_P]};
@@ -1054,9 +1130,10 @@ cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
     }
     return cudaErrorInvalidValue;
 }
+bool adj_split() { return BEHF_ADJ_SPLIT != 0; }
 template <class S>
 bool adj_snap_staged() {
-    return BEHF_ADJ_SNAP && sizeof(S) == 2;
+    return BEHF_ADJ_SPLIT || (BEHF_ADJ_SNAP && sizeof(S) == 2);
 }
 template <class S>
 cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv) {

@@ -26,6 +26,8 @@ struct AdjPtrs {
     void* tmpT[7];           // per-cell derivative-group adjoints of T^T and V^T, type A, pitched
     void* tmpV[6];           // (zero off the updated cells)
     void* g[kNCoef];         // gradient accumulators per effective coefficient, type A, pitched
+    void* mu[3];             // mu = lq' - VU2 lv' of V^T per cell outside the slabs, type A, pitched (for the
+                             // separate gradient kernels)
     const void* cur[kNField];  // forward snapshot of this step after V (and the force source), type S
     const void* qprev[3];    // q before V of this step, type S
     const void* vq1[6];      // vx vy vz qx qy qz after V of step n - 1 (the fused T^T of that step), type S
@@ -56,6 +58,8 @@ cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m);
 // of the step), mv over its velocities and Darcy velocities (the fused T^T of the step before).
 template <class S>
 bool adj_snap_staged();
+// The coefficient gradients run in launches of their own (two more per step) rather than inside the gathers.
+bool adj_split();
 template <class S>
 cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv);
 // T^T per cell of the first backward step (after its record^T).

@@ -1022,6 +1022,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     for (int q = 0; q < 7 && !st; q++) st = buf.get(&a.tmpT[q], nf * asz);
     for (int q = 0; q < 6 && !st; q++) st = buf.get(&a.tmpV[q], nf * asz);
     for (int q = 0; q < kNCoef && !st; q++) st = buf.get(&a.g[q], nf * asz);
+    for (int q = 0; q < 3 && !st; q++) st = buf.get(&a.mu[q], nf * asz);
     if (g.W > 0)
         for (int ax = 0; ax < 3 && !st; ax++)
             for (int s = 0; s < 8 && !st; s++) {
@@ -1226,7 +1227,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                            fuse, c->stream));
             CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
             if (fuse) CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc, c->stream));
-            c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse;
+            c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
         }
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
