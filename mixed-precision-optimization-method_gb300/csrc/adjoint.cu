@@ -265,7 +265,7 @@ constexpr int GX = 32, GY = 8;
 #endif
 // the split V^T gather (T-slot memory and T^T per cell of the next step): its CTAs per SM
 #ifndef BEHF_ADJ_MINB_G1
-#define BEHF_ADJ_MINB_G1 2
+#define BEHF_ADJ_MINB_G1 3
 #endif
 
 struct StageSet {
@@ -726,8 +726,9 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                 A lo[7];  // sxx syy szz sxy sxz syz p
 #pragma unroll
                 for (int q = 0; q < 7; q++) lo[q] = Q::ad(a.lf[BEHF_SXX + q])[c];
-                // T-slot adjoint memory of this step on slab cells (its gathers ran in the KIND 0 launch)
-                const bool mem = !inner;
+                // T-slot adjoint memory of this step on slab cells (its gathers ran in the KIND 0 launch), here in
+                // the fused mode; the split mode updates it in its own launch before this one
+                const bool mem = MODE == 0 && !inner;
                 A tt[7];
                 MemUpd<A, 4, 0xC> mt;
                 if (mem) {
@@ -739,7 +740,7 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                 // slabs the forward derivatives of step n - 1 and the gradient accumulators
                 A kc[8];
                 if (fuse) t_coefs<S, R>(g, p, a, c, kc);
-                const bool gr = MODE == 0 && fuse && a.grad && !mem;
+                const bool gr = MODE == 0 && fuse && a.grad && inner;
                 A du[10], go[8];
                 if (gr) {
                     v_stencils(du);
@@ -793,9 +794,11 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
 #undef CELL_INDEX
 
 // V-slot adjoint memory update of one step on the slab cells of the updated region, one slab cell of one axis per
-// thread (a cell in two slabs is visited once per axis): from the cell's tmpV, the slots 0..3 of that axis.
+// thread (a cell in two slabs is visited once per axis): from the cell's tmpV, the slots 0..3 of that axis
+// (TSLOT 0); or, TSLOT 1, the T-slot update from tmpT, slots 4..7 (split gathers: after the T^T gather that reads
+// those slots, before the V^T gather overwrites tmpT with the next step's).
 __device__ __forceinline__ int slab_pos(int s, int n, int L) { return s < L ? s : n - 1 - L + (s - L); }
-template <class A>
+template <class A, int TSLOT>
 __global__ void k_vmem(Geom g, DevPtrs p, AdjPtrs a) {
     const long long n0 = (long long)g.nz * g.ny * g.W, n1 = (long long)g.nz * g.W * g.nx;
     const long long n2 = (long long)g.W * g.ny * g.nx, tot = n0 + n1 + n2;
@@ -826,23 +829,27 @@ __global__ void k_vmem(Geom g, DevPtrs p, AdjPtrs a) {
         }
         if (i < g.R || i >= g.nx - g.R || j < g.R || j >= g.ny - g.R || k < g.R || k >= g.nz - g.R) continue;
         const long long c = (long long)k * g.plane + (long long)j * g.px + i;
-        // axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
-        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y
-        const int dq[4] = {ax, ax + 3, ax == 0 ? 1 : 0, ax == 2 ? 1 : 2};
+        // V slots, axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
+        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y.  T slots, axis x: uxx s4, wx s5, uyx s6h, uzx s7h; y: uyy, wy,
+        // uxy, uzy; z: uzz, wz, uxz, uyz (tmpT 0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz)
+        const int dq[4] = {ax, TSLOT ? 3 : ax + 3, TSLOT ? (ax == 2 ? 5 : 4) : (ax == 0 ? 1 : 0),
+                           TSLOT ? (ax == 0 ? 5 : 6) : (ax == 2 ? 1 : 2)};
+        constexpr int SB = TSLOT ? 4 : 0;
         A D[4], L[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            D[q] = reinterpret_cast<const A*>(a.tmpV[dq[q]])[c];
-            L[q] = reinterpret_cast<const A*>(a.lpsi[ax][q])[u];
+            D[q] = reinterpret_cast<const A*>(TSLOT ? a.tmpT[dq[q]] : a.tmpV[dq[q]])[c];
+            L[q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[u];
         }
         const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
         const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const A Ap = q < 2 ? pa2 : pa, B = q < 2 ? pb2 : pb;
+            const bool h = TSLOT ? q >= 2 : q < 2;  // half-shifted profiles: V slots 0, 1; T slots 6, 7
+            const A Ap = h ? pa2 : pa, B = h ? pb2 : pb;
             const A Lm = L[q] + D[q];
-            reinterpret_cast<A*>(a.lpsi[ax][q])[u] = Ap * Lm;
-            reinterpret_cast<A*>(a.lprv[ax][q])[u] = Ap * B * Lm;
+            reinterpret_cast<A*>(a.lpsi[ax][SB + q])[u] = Ap * Lm;
+            reinterpret_cast<A*>(a.lprv[ax][SB + q])[u] = Ap * B * Lm;
         }
     }
 }
@@ -1056,20 +1063,13 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
     if ((split || GMap<S, R, 0>::SNAP) && a.grad && (!snapT || (fuse && !snapV))) return cudaErrorInvalidValue;
     // T^T gather + V^T; its V-coefficient gradients; V^T gather + T-slot memory + T^T of step n - 1; its
     // T-coefficient gradients
+    typedef typename Traits<S>::C A;
     k_gather<S, R, 0, MG><<<ggrid, block, smemg, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0);
     if (split && a.grad) k_gather<S, R, 0, 2><<<ggrid, block, smemd, st>>>(m.t, *snapT, g, p, a, t, zc, 0);
+    if (split && g.W > 0) k_vmem<A, 1><<<sms * 8, 256, 0, st>>>(g, p, a);
     k_gather<S, R, 1, MG><<<ggrid, block, smemg, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse);
     if (split && a.grad && fuse) k_gather<S, R, 1, 2><<<ggrid, block, smemd, st>>>(m.v, *snapV, g, p, a, v, zc, fuse);
-    if (g.W > 0) {
-        static int sms = 0;
-        if (sms == 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (sms <= 0) sms = 148;
-        }
-        k_vmem<typename Traits<S>::C><<<sms * 8, 256, 0, st>>>(g, p, a);
-    }
+    if (g.W > 0) k_vmem<A, 0><<<sms * 8, 256, 0, st>>>(g, p, a);
     return cudaGetLastError();
 }
 
