@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "behf.h"
 
 namespace behf {
@@ -118,29 +120,29 @@ __host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
 // z planes per CTA of a z-marching launch over nxy tiles and `planes` planes with `slots` CTAs resident per
 // wave: the chunk length in [minz, maxz] minimising (waves, rounded up) x (chunk + halo), so that the last wave
 // is not left mostly empty (a wave's time is set by its longest CTA) and short chunks do not repeat the halo
-// planes' warm-up too often; with at least minw waves where the chunk range allows it (more, shorter CTAs even
-// out tiles of unequal cost).  Ties go to the longer chunk.
+// planes' warm-up too often; among the chunk lengths that give at least minw waves, or as many CTAs as the
+// shortest chunk gives when that is fewer (more, shorter CTAs even out tiles of unequal cost).  Ties go to the
+// longer chunk.
 inline int wave_zchunk(int nxy, int planes, int slots, int minz, int maxz, int halo, int minw = 1) {
     if (planes <= 0) return 1;
     if (minz < 1) minz = 1;
     if (maxz < minz) maxz = minz;
     const int cmax = planes / minz > 1 ? planes / minz : 1;
+    const long long nmax = (planes + (planes + cmax - 1) / cmax - 1) / ((planes + cmax - 1) / cmax);
+    const long long floor_ctas = std::min((long long)minw * slots, (long long)nxy * nmax);
     int best = planes < maxz ? planes : maxz;
-    for (int pass = 0; pass < 2; pass++) {  // pass 0 with the wave floor, pass 1 without it
-        long long bestcost = -1;
-        for (int nch = 1; nch <= cmax; nch++) {
-            const int zc = (planes + nch - 1) / nch;
-            if (zc > maxz) continue;
-            const long long n = (planes + zc - 1) / zc;
-            if (pass == 0 && (long long)nxy * n < (long long)minw * slots) continue;
-            const long long waves = ((long long)nxy * n + slots - 1) / slots;
-            const long long cost = waves * (zc + halo);
-            if (bestcost < 0 || cost < bestcost) {
-                bestcost = cost;
-                best = zc;
-            }
+    long long bestcost = -1;
+    for (int nch = 1; nch <= cmax; nch++) {
+        const int zc = (planes + nch - 1) / nch;
+        if (zc > maxz) continue;
+        const long long n = (planes + zc - 1) / zc;
+        if ((long long)nxy * n < floor_ctas) continue;
+        const long long waves = ((long long)nxy * n + slots - 1) / slots;
+        const long long cost = waves * (zc + halo);
+        if (bestcost < 0 || cost < bestcost) {
+            bestcost = cost;
+            best = zc;
         }
-        if (bestcost >= 0) break;
     }
     return best;
 }

@@ -612,9 +612,11 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // z chunks of at most BEHF_TILED_ZCHUNK planes: short z ranges keep the CTAs that share halo rows marching the
     // same planes at the same time, so the rows one CTA brings into L2 are still there when its neighbours read
     // them (measured at 1024^3 FP16: 64-plane chunks 34.7 ms per step against 40.2 ms for whole columns); within
-    // that, a chunk count that fills the last wave of resident CTAs (MINB per SM)
+    // that, a chunk count that fills the last wave of resident CTAs (MINB per SM) with at least four waves where
+    // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
+    // for two waves of 36-plane chunks)
     const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
-    int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R);
+    int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, 4);
     if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
