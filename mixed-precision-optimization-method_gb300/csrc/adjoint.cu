@@ -257,6 +257,11 @@ constexpr int GX = 32, GY = 8;
 #endif
 // 1: the coefficient gradients run in kernels of their own (MODE 2) after register-lean gathers (MODE 1), at
 // BEHF_ADJ_MINB_SPLIT CTAs per SM; 0: fused into the gathers (MODE 0).
+// at least this many waves of gather CTAs where the z chunking allows it (measured at 256^3, 600-step gradient:
+// 4 waves 2.43 s, 8 waves 2.35 s, 16 waves 2.36 s)
+#ifndef BEHF_ADJ_MINW
+#define BEHF_ADJ_MINW 8
+#endif
 #ifndef BEHF_ADJ_SPLIT
 #define BEHF_ADJ_SPLIT 1
 #endif
@@ -1028,10 +1033,12 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    // z chunks (2 CTAs per SM resident) that fill the last wave, at most 64 planes, at least 4 waves (measured at
-    // 192^3: 2 waves of 46-plane chunks 553 + 615 us per step, 5 waves of 17 planes 521 + 522 us)
+    // z chunks that fill the last wave of resident CTAs, at most 64 planes, at least BEHF_ADJ_MINW waves (measured
+    // at 192^3 with the fused gathers: 2 waves of 46-plane chunks 553 + 615 us per step, 5 waves of 17 planes
+    // 499 + 516 us)
     const int nxy = (int)(((nxu + GX - 1) / GX) * ((nyu + GY - 1) / GY));
-    const int zc = wave_zchunk(nxy, nzu, 2 * sms, 8, 64, R, 4);
+    const int resident = BEHF_ADJ_SPLIT ? BEHF_ADJ_MINB_SPLIT : BEHF_ADJ_MINB;
+    const int zc = wave_zchunk(nxy, nzu, resident * sms, 8, 64, R, BEHF_ADJ_MINW);
     const dim3 ggrid((nxu + GX - 1) / GX, (nyu + GY - 1) / GY, (nzu + zc - 1) / zc);
     StageSet t{}, v{};
     // T^T gather: x {T0 s4, T4 s6h, T5 s7h, T3 s5}, y {T1 s4, T4 s6h, T6 s7h, T3 s5}, z {T2 s4, T5 s6h, T6 s7h, T3 s5}

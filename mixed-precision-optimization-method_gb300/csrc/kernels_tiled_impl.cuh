@@ -31,6 +31,10 @@ namespace tiled {
 #ifndef BEHF_TILED_VLOAD_EARLY16
 #define BEHF_TILED_VLOAD_EARLY16 0
 #endif
+// At least this many waves of resident CTAs where 16-plane z ranges allow it.
+#ifndef BEHF_TILED_MINW
+#define BEHF_TILED_MINW 4
+#endif
 // Longest z range a CTA marches by default (BEHF_OPT_ZCHUNK overrides it).
 #ifndef BEHF_TILED_ZCHUNK
 #define BEHF_TILED_ZCHUNK 64
@@ -616,7 +620,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
     // for two waves of 36-plane chunks)
     const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
-    int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, 4);
+    int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, BEHF_TILED_MINW);
     if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
