@@ -268,6 +268,11 @@ constexpr int GX = 32, GY = 8;
 #ifndef BEHF_ADJ_MINB_SPLIT
 #define BEHF_ADJ_MINB_SPLIT 3
 #endif
+// the split gradient kernels (MODE 2): their CTAs per SM (41 KB of shared memory each; measured at 256^3, 600-step
+// gradient: 3 per SM 2.37 s, 4 per SM 2.34 s, 5 per SM, spilling, 2.45 s)
+#ifndef BEHF_ADJ_MINB_GRAD
+#define BEHF_ADJ_MINB_GRAD 4
+#endif
 // the split V^T gather (T-slot memory and T^T per cell of the next step): its CTAs per SM
 #ifndef BEHF_ADJ_MINB_G1
 #define BEHF_ADJ_MINB_G1 3
@@ -378,7 +383,9 @@ struct GMap {
 // snapshot arrays (SNAP only).
 template <class S, int R, int KIND, int MODE>
 __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
-                                       : (MODE == 1 && KIND == 1) ? BEHF_ADJ_MINB_G1 : BEHF_ADJ_MINB_SPLIT)
+                                       : MODE == 2                ? BEHF_ADJ_MINB_GRAD
+                                       : KIND == 1                ? BEHF_ADJ_MINB_G1
+                                                                  : BEHF_ADJ_MINB_SPLIT)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
              AdjPtrs a, StageSet ss, int zc, int fuse) {
     typedef GatherOps<S, R> W;
