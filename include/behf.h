@@ -102,6 +102,9 @@ enum {
     BEHF_OPT_SNAPSHOT_CACHE = 8, /* gradient: device memory for keeping the forward pass's per-step snapshots of the
                                     last checkpoint segments, which then need no recompute (-1 = automatic: the free
                                     memory but max(8 GiB, 10 % of the device); 0 = none; n > 0 = at most n MiB) */
+    BEHF_OPT_CHECKPOINT_OUTER = 9, /* gradient: outer checkpoint spacing of the two-level scheme, rounded up to a
+                                    multiple of BEHF_OPT_CHECKPOINT (0 = automatic: one level when it fits the
+                                    device memory, else two levels with the inner spacing halved until they fit) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current

@@ -23,7 +23,7 @@ PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
 (OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
- OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE) = range(9)
+ OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER) = range(10)
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -291,14 +291,16 @@ class Solver:
         return int(self._lib.behf_selftest_wait(self._ctx))
 
     # -- gradient (adjoint state, checkpointed)
-    def enable_gradient(self, checkpoint: int = 0, snapshot_cache: int = -1):
+    def enable_gradient(self, checkpoint: int = 0, snapshot_cache: int = -1, checkpoint_outer: int = 0):
         """Keep the moduli on the device for behf_gradient (call before the medium); checkpoint = steps
         between checkpoints of the gradient's forward pass (0 = round(sqrt(nt))); snapshot_cache = device MiB
         for keeping the forward pass's snapshots of the last segments (-1 automatic, 0 none: every segment is
-        recomputed from its checkpoint)."""
+        recomputed from its checkpoint); checkpoint_outer = outer spacing of the two-level scheme (0 automatic:
+        two levels only when one does not fit the device memory)."""
         self.set_option(OPT_GRADIENT, 1)
         self.set_option(OPT_CHECKPOINT, int(checkpoint))
         self.set_option(OPT_SNAPSHOT_CACHE, int(snapshot_cache))
+        self.set_option(OPT_CHECKPOINT_OUTER, int(checkpoint_outer))
 
     def _grad_out(self, nt, moduli):
         gw = np.zeros(nt, np.float64)
@@ -373,7 +375,7 @@ def run_batch(solvers, nsteps: int):
 
 
 def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None, gradient=False,
-               checkpoint=0, coef_rounding=0, state_rounding=0, snapshot_cache=-1) -> Solver:
+               checkpoint=0, coef_rounding=0, state_rounding=0, snapshot_cache=-1, checkpoint_outer=0) -> Solver:
     """A Solver set up with a problem description (see behf.problems.Problem); gradient=True keeps what
     Solver.gradient needs."""
     s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
@@ -384,7 +386,7 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
         s.set_option(OPT_REF_BUG_COMPAT, 1)
     s.set_kernel(kernel)
     if gradient:
-        s.enable_gradient(checkpoint, snapshot_cache)
+        s.enable_gradient(checkpoint, snapshot_cache, checkpoint_outer)
     if coef_rounding:
         s.set_option(OPT_COEF_ROUNDING, int(coef_rounding))
     if state_rounding:

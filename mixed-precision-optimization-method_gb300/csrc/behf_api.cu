@@ -129,6 +129,7 @@ struct behf_ctx {
     bool keep_medium = false;
     float* d_mod[kNMod] = {};
     int ck_stride = 0;
+    int ck_outer = 0;  // gradient: outer checkpoint spacing of the two-level scheme (0 automatic)
     int snap_cache_mib = -1;  // gradient: device memory for snapshots kept from the forward pass (-1 automatic)
     int coef_dither = 0;  // BEHF_OPT_COEF_ROUNDING
 
@@ -844,6 +845,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative checkpoint spacing");
             c->ck_stride = value;
             break;
+        case BEHF_OPT_CHECKPOINT_OUTER:
+            if (value < 0) return fail(BEHF_ERR_INVALID, "negative outer checkpoint spacing");
+            c->ck_outer = value;
+            break;
         case BEHF_OPT_SNAPSHOT_CACHE:
             if (value < -1) return fail(BEHF_ERR_INVALID, "snapshot cache must be -1 (automatic), 0 or a size in MiB");
             c->snap_cache_mib = value;
@@ -1013,8 +1018,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
     const size_t sl[3] = {(size_t)c->grid.nz * c->grid.ny * g.W, (size_t)c->grid.nz * g.W * c->grid.nx,
                           (size_t)g.W * c->grid.ny * c->grid.nx};
-    const int S_ = c->ck_stride > 0 ? c->ck_stride : std::max(1, (int)std::lround(std::sqrt((double)nt)));
-    const int nseg = (nt + S_ - 1) / S_;
+    int S_ = c->ck_stride > 0 ? c->ck_stride : std::max(1, (int)std::lround(std::sqrt((double)nt)));
     DevBuf buf(c);
     AdjPtrs a{};
     behf_status st = BEHF_OK;
@@ -1034,10 +1038,54 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     if (g.W > 0)
         for (int ax = 0; ax < 3; ax++) ck_bytes += 16 * align256(sl[ax] * c->ws);
     const size_t snap_bytes = kNField * align256(nf * c->es);
+    // Checkpoint scheme.  One level: a full-state checkpoint every S_ steps, each segment recomputed once with its
+    // per-step snapshots (S_ + 1 slots).  Two levels, when that does not fit the device memory or
+    // BEHF_OPT_CHECKPOINT_OUTER asks for it: an outer checkpoint every So_ steps (a multiple of S_); each outer
+    // segment is run forward again from its checkpoint keeping a checkpoint every S_ steps, and those inner
+    // segments are recomputed with snapshots as in one level -- one more forward pass, ceil(nt / So_) + So_ / S_
+    // checkpoints instead of nt / S_.  Automatically the inner spacing halves until the scheme fits.
+    if (st) return st;
+    auto need = [&](int s2, int s1) -> size_t {
+        const size_t nout = (size_t)(nt + s1 - 1) / s1, nin = s1 > s2 ? (size_t)(s1 + s2 - 1) / s2 : 0;
+        return (nout + nin) * ck_bytes + (size_t)(s2 + 1) * snap_bytes + (size_t)c->nrec * nt * 8;
+    };
+    int So_ = S_;
+    if (c->ck_outer > 0) {
+        So_ = (std::max(c->ck_outer, S_) + S_ - 1) / S_ * S_;
+    } else {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const size_t margin = std::max((size_t)2 << 30, tot / 50);
+        const size_t avail = fr > margin ? fr - margin : 0;
+        if (need(S_, S_) > avail) {
+            for (int s2 = S_; s2 >= 1; s2 = c->ck_stride > 0 ? 0 : s2 / 2) {
+                size_t best = 0;
+                int bs1 = s2;
+                for (long long k = 2; k * s2 < 2LL * nt; k++) {
+                    const size_t n = need(s2, (int)(k * s2));
+                    if (!best || n < best) {
+                        best = n;
+                        bs1 = (int)(k * s2);
+                    }
+                }
+                if (best && best <= avail) {
+                    S_ = s2;
+                    So_ = bs1;
+                    break;
+                }
+            }
+            // nothing fits: keep one level, whose allocation below reports the shortfall
+        }
+    }
+    const int nseg = (nt + S_ - 1) / S_;      // snapshot segments (one level: also the checkpoint segments)
+    const int nout = (nt + So_ - 1) / So_;      // outer segments (= nseg with one level)
+    const bool two = So_ > S_;
     char* ck = nullptr;
+    char* ckin = nullptr;  // two levels: the checkpoints inside one outer segment
     char* snap = nullptr;
     double *d_adj = nullptr, *d_gw = nullptr, *d_gfac = nullptr, *d_gm = nullptr;
-    if (!st) st = buf.get((void**)&ck, ck_bytes * nseg);
+    if (!st) st = buf.get((void**)&ck, ck_bytes * nout);
+    if (!st && two) st = buf.get((void**)&ckin, ck_bytes * ((So_ + S_ - 1) / S_));
     if (!st) st = buf.get((void**)&snap, snap_bytes * (S_ + 1));
     if (!st) st = buf.get((void**)&d_adj, (size_t)c->nrec * nt * 8);
     if (!st) st = buf.get((void**)&d_gw, (size_t)nt * 8);
@@ -1067,7 +1115,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     // (BEHF_OPT_SNAPSHOT_CACHE: -1 all of it but max(8 GiB, 10 %), 0 none, else that many MiB); their slot 0 is the
     // segment's checkpoint, which holds the 13 fields in the same layout.  The others share one buffer.
     std::vector<char*> cache(nseg, nullptr);
-    if (c->snap_cache_mib != 0) {
+    if (c->snap_cache_mib != 0 && !two) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
         const size_t margin = std::max((size_t)8 << 30, tot / 10);
@@ -1081,9 +1129,10 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                 break;
             }
     }
+    auto cached = [&](int sg) { return sg >= 0 && cache[sg] != nullptr; };  // sg -1: a segment never cached
     auto snap_ptr = [&](int sg, int idx, int f) -> char* {
         const size_t fo = align256(nf * c->es) * f;
-        if (cache[sg]) return idx == 0 ? ck + ck_bytes * sg + fo : cache[sg] + snap_bytes * (idx - 1) + fo;
+        if (cached(sg)) return idx == 0 ? ck + ck_bytes * sg + fo : cache[sg] + snap_bytes * (idx - 1) + fo;
         return snap + snap_bytes * idx + fo;
     };
     // tensor maps of a segment's snapshot slots (the 16-bit kinds stage snapshot windows in the gathers)
@@ -1091,7 +1140,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     int maps_seg = -2;  // segment whose buffers the maps describe (-1: the shared buffer)
     auto build_snap_maps = [&](int sg) -> cudaError_t {
         if (!adj_snap_staged<S>()) return cudaSuccess;
-        const int key = cache[sg] ? sg : -1;
+        const int key = cached(sg) ? sg : -1;
         if (key == maps_seg) return cudaSuccess;
         snap_mt.resize(S_ + 1);
         snap_mv.resize(S_ + 1);
@@ -1134,6 +1183,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(source_factor(c, &fac));
     const long long so = c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]);
     // one forward step with the d_it counter, keeping the fields after V (+ force) in slot idx of segment sg
+    // (idx < 0: no snapshot)
     auto snap_step = [&](int sg, int idx, bool record) -> cudaError_t {
         cudaError_t e;
         if (c->src_kind != BEHF_SRC_FORCE_Z &&
@@ -1143,7 +1193,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
         if (c->src_kind == BEHF_SRC_FORCE_Z &&
             (e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
             return e;
-        if ((e = snap_fields(sg, idx)) != cudaSuccess) return e;
+        if (idx >= 0 && (e = snap_fields(sg, idx)) != cudaSuccess) return e;
         if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
         if (record) {
             RecScales rs;
@@ -1159,10 +1209,10 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     // forward pass with checkpoints (seismograms recorded as in behf_run); cached segments step by step
     st = zero_state(c);
     if (st) return st;
-    for (int sg = 0; sg < nseg; sg++) {
-        const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
+    for (int sg = 0; sg < nout; sg++) {
+        const int s0 = sg * So_, s1 = std::min(nt, s0 + So_);
         CK(copy_state(ck + ck_bytes * sg, true));
-        if (!cache[sg]) {
+        if (!cached(sg)) {
             st = behf_run_async(c, s1 - s0);
             if (st) return st;
         } else {
@@ -1200,10 +1250,24 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     for (int q = 0; q < kNField; q++) sc.s[q] = alpha / c->field_scale(q);
     CK(cudaMemcpy(d_adj, adj.data(), adj.size() * 8, cudaMemcpyHostToDevice));
 
-    for (int sg = nseg - 1; sg >= 0; sg--) {
-        const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
-        if (!cache[sg]) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
-            CK(copy_state(ck + ck_bytes * sg, false));
+    for (int og = nout - 1; og >= 0; og--) {
+      const int o0 = og * So_, o1 = std::min(nt, o0 + So_);
+      const int nin = two ? (o1 - o0 + S_ - 1) / S_ : 1;
+      if (two) {  // run the outer segment forward again from its checkpoint, keeping a checkpoint every S_ steps
+          CK(copy_state(ck + ck_bytes * og, false));
+          CK(cudaMemcpyAsync(c->d_it, &o0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+          CK(cudaStreamSynchronize(c->stream));
+          for (int j = 0; j < nin; j++) {
+              CK(copy_state(ckin + ck_bytes * j, true));
+              for (int it = o0 + j * S_; it < std::min(o1, o0 + (j + 1) * S_); it++) CK(snap_step(-1, -1, false));
+          }
+      }
+      for (int j = nin - 1; j >= 0; j--) {
+        const int sg = two ? -1 : og;  // the segment's index in the snapshot cache (never cached with two levels)
+        const int s0 = o0 + j * S_, s1 = std::min(o1, s0 + S_);
+        char* ckp = two ? ckin + ck_bytes * j : ck + ck_bytes * og;
+        if (!cached(sg)) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
+            CK(copy_state(ckp, false));
             CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
             CK(cudaStreamSynchronize(c->stream));
             CK(snap_fields(sg, 0));
@@ -1229,6 +1293,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             if (fuse) CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc, c->stream));
             c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
         }
+      }
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     st = behf_sync(c);

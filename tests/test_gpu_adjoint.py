@@ -1,8 +1,8 @@
 """Adjoint-state gradient on the GPU (behf_gradient / behf_misfit_gradient through the C ABI), against the
 FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identity and finite differences):
   * FP64: wavelet and moduli gradients within 1e-9 relative L2 of the oracle, every source kind, radius 1/2/4,
-    with and without CPML; dot-product identity within 1e-10; checkpoint spacing and the snapshot cache change
-    nothing;
+    with and without CPML; dot-product identity within 1e-10; checkpoint spacing, two checkpoint levels and the
+    snapshot cache change nothing;
   * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
   * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
 from __future__ import annotations
@@ -32,9 +32,9 @@ def rel(a, b):
     return np.linalg.norm((a - b).ravel()) / d if d > 0 else np.linalg.norm(a.ravel())
 
 
-def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto", snapshot_cache=-1):
+def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto", snapshot_cache=-1, checkpoint_outer=0):
     s = behf.solver_for(p, precision=precision, kernel=kernel, gradient=True, checkpoint=checkpoint,
-                        snapshot_cache=snapshot_cache)
+                        snapshot_cache=snapshot_cache, checkpoint_outer=checkpoint_outer)
     gw, gm = s.gradient(p.nt, adj)
     seis = s.seismograms()
     s.close()
@@ -94,6 +94,10 @@ def test_gradient_snapshot_cache(behf_lib, precision):
         out = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=cache)
         for a, b in zip(out, ref):
             np.testing.assert_array_equal(a, b)
+    # two checkpoint levels (outer segments of 39 = 3 x 13 steps, each run again for its inner checkpoints)
+    out = gpu_gradient(p, adj, precision, checkpoint=13, checkpoint_outer=30)
+    for a, b in zip(out, ref):
+        np.testing.assert_array_equal(a, b)
 
 
 @pytest.mark.parametrize("precision,tol", [("f32", 1e-4), ("f16", 5e-2)])
