@@ -62,3 +62,27 @@ def test_run_batch_matches_sequential(behf_lib):
     for s, ref in zip(solvers, seq):
         np.testing.assert_array_equal(s.seismograms(), ref)
         s.close()
+
+
+@pytest.mark.parametrize("precision", ["f16", "bf16", "f32"])
+def test_run_batch_same_grid_in_two_calls(behf_lib, precision):
+    # three shots of one grid: different source kinds and positions, a layered medium for one, stochastic
+    # rounding of the stored fields for another (16-bit kinds); batched in two calls (40 + 21 steps: graph
+    # chunks of 16 and remainders), against each shot alone
+    kinds = ["explosive", "pressure", "force_z"]
+    probs = [dataclasses.replace(shot(i, nt=61), src_kind=kinds[i]) for i in range(3)]
+    probs[2] = dataclasses.replace(probs[2], mod=P.layered((48, 48, 48), [P.SANDSTONE, P.STIFF], [24]))
+    sr = [0, 1 if precision != "f32" else 0, 0]
+    seq = []
+    for p, r in zip(probs, sr):
+        s = behf.solver_for(p, precision=precision, state_rounding=r)
+        s.run(p.nt)
+        seq.append(s.seismograms())
+        s.close()
+    solvers = [behf.solver_for(p, precision=precision, state_rounding=r) for p, r in zip(probs, sr)]
+    behf.run_batch(solvers, 40)
+    behf.run_batch(solvers, 21)
+    for s, ref in zip(solvers, seq):
+        assert s.info()["step"] == 61
+        np.testing.assert_array_equal(s.seismograms(), ref)
+        s.close()
