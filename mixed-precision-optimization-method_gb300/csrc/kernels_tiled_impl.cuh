@@ -25,11 +25,19 @@ namespace tiled {
 #ifndef BEHF_TILED_MINB32
 #define BEHF_TILED_MINB32 1
 #endif
-// Velocity kernel, 16-bit kinds: 1 issues the cell's own loads before the pipeline waits (their latency overlaps
-// the waits, but 21 more registers stay live), 0 after the stencils (fits 80 registers; the best choice at 3 CTAs
-// per SM).  FP32 (1 CTA per SM) always issues them early.
+// Velocity kernel, 16-bit kinds: the groups of the cell's own loads issued before the pipeline waits (their latency
+// overlaps the waits, but their registers stay live through the stencils), the rest after the stencils: a mask of
+// 1 = v and q, 2 = VW1 (FP32), 4 = VW3, VU1, VU2.  0 (all after) fits 80 registers; 7 spills at 3 CTAs per SM.
+// Measured at 1024^3 FP16 on one GPU: 0 17.79 ms, 1 19.52, 2 18.56, 4 18.42.  FP32 (1 CTA per SM) always issues
+// them early.
 #ifndef BEHF_TILED_VLOAD_EARLY16
 #define BEHF_TILED_VLOAD_EARLY16 0
+#endif
+// Stress kernel, 16-bit kinds: the cell's own stresses/pressure and coefficients are loaded 0 before the pipeline
+// waits, 1 after the stencils, 2 fields before and coefficients after (1024^3 FP16, one GPU: 16.18, 17.67 and
+// 17.85 ms; all three at 80 registers without spills).  FP32 always loads them early.
+#ifndef BEHF_TILED_SLOAD16
+#define BEHF_TILED_SLOAD16 0
 #endif
 // At least this many waves of resident CTAs where 16-plane z ranges allow it.
 #ifndef BEHF_TILED_MINW
@@ -298,19 +306,25 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
         P vo_s[3], qo_s[3];
         float2 vw1[3];
         KP kw3[3], ku1[3], ku2[3];
-        auto load_own = [&]() {
+        // groups: 1 = v, q; 2 = VW1; 4 = VW3, VU1, VU2
+        auto load_own = [&](int groups) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
-                qo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_QX + a]) + go);
-                vw1[a] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.k[VW1X + a]) + go);
-                kw3[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VW3X + a]) + go);
-                ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
-                ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
+                if (groups & 1) {
+                    vo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_VX + a]) + go);
+                    qo_s[a] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_QX + a]) + go);
+                }
+                if (groups & 2)
+                    vw1[a] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(p.k[VW1X + a]) + go);
+                if (groups & 4) {
+                    kw3[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VW3X + a]) + go);
+                    ku1[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU1X + a]) + go);
+                    ku2[a] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[VU2X + a]) + go);
+                }
             }
         };
-        constexpr bool early = sizeof(S) == 4 || BEHF_TILED_VLOAD_EARLY16;
-        if (early && live) load_own();
+        constexpr int early = sizeof(S) == 4 ? 7 : BEHF_TILED_VLOAD_EARLY16;
+        if (early && live) load_own(early);
         bool ok = true;
         if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
         if (ok) ok = mbar_wait(&bfull[st], (pp.fph >> st) & 1u);
@@ -373,7 +387,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
-            if (!early) load_own();
+            if (early != 7) load_own(7 & ~early);
             auto km = [&](KP kv, int j) { return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j])); };
 #pragma unroll
             for (int a = 0; a < 3; a++) {
@@ -471,13 +485,22 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
         const long long go = (long long)k * g.plane + col;
         P so_s[7];
         KP kk[7];
-        if (live) {
+        constexpr int smode = sizeof(S) == 4 ? 0 : BEHF_TILED_SLOAD16;
+        auto load_fields = [&]() {
+#pragma unroll
+            for (int q = 0; q < 7; q++)
+                so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
+        };
+        auto load_coefs = [&]() {
 #pragma unroll
             for (int q = 0; q < 7; q++) {
-                so_s[q] = *reinterpret_cast<const P*>(reinterpret_cast<const S*>(p.f[BEHF_SXX + q]) + go);
                 const int j = q < 4 ? P1 + q : P1 + q + 1;
                 kk[q] = *reinterpret_cast<const KP*>(reinterpret_cast<const K*>(p.k[j]) + go);
             }
+        };
+        if (live) {
+            if (smode != 1) load_fields();
+            if (smode == 0) load_coefs();
         }
         bool ok = true;
         if (tid == 0) ok = producer_step<M>(pp, it, k, kb, ke, issue);
@@ -537,6 +560,8 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
                 const bool hf[4] = {false, false, true, true};
                 pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
             }
+            if (smode == 1) load_fields();
+            if (smode != 0) load_coefs();
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);
             auto kc = [&](int q) {
