@@ -1,15 +1,15 @@
 // kernels_tiled.cuh -- z-marching velocity / stress kernels for sm_103a (FP16, BF16, FP32 storage).
 //
 // One CTA owns an xy tile of TXC x TY cells (64 x 8; 256 threads, each thread a pair of adjacent x cells,
-// one warp per tile row) and marches it through z, one plane per step:
-//   * the fields with a z-derivative live in a register queue of the 2R+1 planes around the current one,
-//     refilled by one coalesced load per step (the reference re-reads every neighbour from HBM,
-//     kernel.cu:172-185);
-//   * everything else for plane k -- the xy-halo boxes of the fields with x/y derivatives, the cell's own
-//     fields and its coefficients -- arrives by TMA (cp.async.bulk.tensor.3d) into a two-stage shared-
-//     memory ring, signalled by an mbarrier; the copies for plane k+1 are in flight while plane k is
-//     computed.  Halo boxes start on 16-byte x boundaries (x0 - 16 B) and TMA zero-fills outside the
-//     grid, which provides the ghost zeros of the domain faces;
+// one warp per tile row) and marches it through a range of z planes, one plane per iteration:
+//   * thread 0 issues TMA copies (cp.async.bulk.tensor.3d) for plane k + 1 while plane k is computed: the
+//     xy-halo boxes of the fields with x/y derivatives into a two-stage shared-memory ring, and the next plane
+//     of each field with a z derivative into a z ring of 2R + 2 planes (the reference re-reads every
+//     neighbour from HBM, kernel.cu:172-185); full/empty mbarriers pipeline the stages.  Halo boxes start on
+//     16-byte x boundaries (x0 - 16 B) and TMA zero-fills outside the grid, which provides the ghost zeros of
+//     the domain faces;
+//   * the cell's own fields and coefficients are coalesced pair loads from global memory (each is read by one
+//     thread only), issued where they hide best: before the waits (stress) or after the stencils (velocity);
 //   * x/y/z stencils are evaluated on cell pairs with packed FP32 arithmetic (fma.rn.f32x2);
 //   * CPML memory is touched only on slab cells (z: block-uniform, y: warp-uniform, x: per cell).
 // Every mbarrier wait is bounded: on timeout the CTA sets the context's error word, drains its
