@@ -18,6 +18,7 @@
 #ifndef BEHF_H
 #define BEHF_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -237,6 +238,18 @@ behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, doubl
  * enqueuing graph-chunk-sized pieces round-robin on their own streams so the shots overlap on the device, then
  * waits for all.  Equivalent to behf_run on each context in turn. */
 behf_status behf_run_batch(behf_ctx* const* ctxs, int n, int nsteps);
+
+/* Checkpoint plan of behf_gradient (host arithmetic only, no context or device): the inner spacing (steps between
+ * the checkpoints that are recomputed with per-step snapshots) and the outer spacing (== inner: one level; a
+ * multiple of it: two levels, each outer segment run forward again for its inner checkpoints) of a gradient over
+ * nt steps, and the device bytes they take.  checkpoint / checkpoint_outer are BEHF_OPT_CHECKPOINT /
+ * BEHF_OPT_CHECKPOINT_OUTER (0 = automatic: inner round(sqrt(nt)); two levels only when one needs more than
+ * avail bytes, the inner spacing then halving until the outer spacing that needs the least memory fits).
+ * ck_bytes / snap_bytes: one checkpoint (13 fields + CPML memory) / one snapshot (13 fields); fixed_bytes: the
+ * rest that scales with nt (the adjoint source).  behf_gradient calls it with the free device memory less
+ * max(2 GiB, 2 %). */
+behf_status behf_checkpoint_plan(int nt, int checkpoint, int checkpoint_outer, size_t ck_bytes, size_t snap_bytes,
+                                 size_t fixed_bytes, size_t avail, int* inner, int* outer, size_t* bytes);
 
 /* Self-test of failure detection (no counterpart in the reference): launches on the context's stream one block
  * that waits, with the bounded wait of the TMA pipelines (about 2 s), on a barrier that nothing releases, then

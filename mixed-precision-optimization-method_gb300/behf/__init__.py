@@ -120,6 +120,8 @@ def load() -> C.CDLL:
         "behf_autotune": [C.c_void_p, C.c_int, P(C.c_int), P(C.c_double)],
         "behf_selftest_wait": [C.c_void_p],
         "behf_run_batch": [P(C.c_void_p), C.c_int, C.c_int],
+        "behf_checkpoint_plan": [C.c_int, C.c_int, C.c_int, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t,
+                                 P(C.c_int), P(C.c_int), P(C.c_size_t)],
         "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                     C.c_void_p, C.c_void_p, C.c_void_p],
     }
@@ -368,6 +370,17 @@ def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:
     return {"velocity": vel, "stress": strs, "step_unfused": vel + strs, "step_fused": fused}
 
 
+def checkpoint_plan(nt: int, ck_bytes: int, snap_bytes: int, avail: int, checkpoint: int = 0,
+                    checkpoint_outer: int = 0, fixed_bytes: int = 0) -> tuple[int, int, int]:
+    """The gradient's checkpoint plan (behf_checkpoint_plan; no GPU needed): (inner spacing, outer spacing, device
+    bytes); outer == inner means one level."""
+    inner, outer, nbytes = C.c_int(), C.c_int(), C.c_size_t()
+    _check(load().behf_checkpoint_plan(int(nt), int(checkpoint), int(checkpoint_outer), int(ck_bytes),
+                                       int(snap_bytes), int(fixed_bytes), int(avail), C.byref(inner),
+                                       C.byref(outer), C.byref(nbytes)))
+    return inner.value, outer.value, nbytes.value
+
+
 def run_batch(solvers, nsteps: int):
     """Advance independent solvers (shots) together on the device: their streams overlap."""
     arr = (C.c_void_p * len(solvers))(*[s._ctx.value for s in solvers])
@@ -401,4 +414,5 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
     return s
 
 
-__all__ = ["Solver", "BehfError", "solver_for", "run_batch", "load", "lib_path", "FIELDS", "FIELD", "MODULI"]
+__all__ = ["Solver", "BehfError", "solver_for", "run_batch", "checkpoint_plan", "load", "lib_path", "FIELDS", "FIELD",
+           "MODULI"]

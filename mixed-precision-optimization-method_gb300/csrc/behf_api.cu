@@ -750,6 +750,47 @@ behf_status behf_run_async(behf_ctx* c, int nsteps) {
     return BEHF_OK;
 }
 
+behf_status behf_checkpoint_plan(int nt, int checkpoint, int checkpoint_outer, size_t ck_bytes, size_t snap_bytes,
+                                 size_t fixed_bytes, size_t avail, int* inner, int* outer, size_t* bytes) {
+    if (nt < 1 || checkpoint < 0 || checkpoint_outer < 0 || !inner || !outer)
+        return fail(BEHF_ERR_INVALID, "bad checkpoint plan arguments");
+    // memory of inner spacing s2 under outer spacing s1 (s1 == s2: one level)
+    auto need = [&](int s2, int s1) -> size_t {
+        const size_t nout = (size_t)(nt + s1 - 1) / s1, nin = s1 > s2 ? (size_t)(s1 + s2 - 1) / s2 : 0;
+        return (nout + nin) * ck_bytes + (size_t)(s2 + 1) * snap_bytes + fixed_bytes;
+    };
+    int S = checkpoint > 0 ? checkpoint : std::max(1, (int)std::lround(std::sqrt((double)nt)));
+    S = std::min(S, nt);
+    int So = S;
+    if (checkpoint_outer > 0) {
+        So = (std::max(checkpoint_outer, S) + S - 1) / S * S;
+    } else if (need(S, S) > avail) {
+        // two levels: the inner spacing halves (unless BEHF_OPT_CHECKPOINT fixes it) until, for the outer spacing
+        // k S that needs the least memory, the scheme fits
+        for (int s2 = S; s2 >= 1; s2 = checkpoint > 0 ? 0 : s2 / 2) {
+            size_t best = 0;
+            int bs1 = s2;
+            for (long long k = 2; k * s2 < 2LL * nt; k++) {
+                const size_t n = need(s2, (int)(k * s2));
+                if (!best || n < best) {
+                    best = n;
+                    bs1 = (int)(k * s2);
+                }
+            }
+            if (best && best <= avail) {
+                S = s2;
+                So = bs1;
+                break;
+            }
+        }
+        // nothing fits: one level, whose allocation reports the shortfall
+    }
+    *inner = S;
+    *outer = So;
+    if (bytes) *bytes = need(S, So);
+    return BEHF_OK;
+}
+
 behf_status behf_sync(behf_ctx* c) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
     CK(cudaStreamSynchronize(c->stream));
@@ -1038,44 +1079,22 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     if (g.W > 0)
         for (int ax = 0; ax < 3; ax++) ck_bytes += 16 * align256(sl[ax] * c->ws);
     const size_t snap_bytes = kNField * align256(nf * c->es);
-    // Checkpoint scheme.  One level: a full-state checkpoint every S_ steps, each segment recomputed once with its
-    // per-step snapshots (S_ + 1 slots).  Two levels, when that does not fit the device memory or
-    // BEHF_OPT_CHECKPOINT_OUTER asks for it: an outer checkpoint every So_ steps (a multiple of S_); each outer
-    // segment is run forward again from its checkpoint keeping a checkpoint every S_ steps, and those inner
-    // segments are recomputed with snapshots as in one level -- one more forward pass, ceil(nt / So_) + So_ / S_
-    // checkpoints instead of nt / S_.  Automatically the inner spacing halves until the scheme fits.
+    // Checkpoint scheme (behf_checkpoint_plan): one level, or two when one does not fit the free device memory
+    // less max(2 GiB, 2 %) or BEHF_OPT_CHECKPOINT_OUTER asks for it.
     if (st) return st;
-    auto need = [&](int s2, int s1) -> size_t {
-        const size_t nout = (size_t)(nt + s1 - 1) / s1, nin = s1 > s2 ? (size_t)(s1 + s2 - 1) / s2 : 0;
-        return (nout + nin) * ck_bytes + (size_t)(s2 + 1) * snap_bytes + (size_t)c->nrec * nt * 8;
-    };
-    int So_ = S_;
-    if (c->ck_outer > 0) {
-        So_ = (std::max(c->ck_outer, S_) + S_ - 1) / S_ * S_;
-    } else {
+    size_t avail = 0;
+    if (c->ck_outer <= 0) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
         const size_t margin = std::max((size_t)2 << 30, tot / 50);
-        const size_t avail = fr > margin ? fr - margin : 0;
-        if (need(S_, S_) > avail) {
-            for (int s2 = S_; s2 >= 1; s2 = c->ck_stride > 0 ? 0 : s2 / 2) {
-                size_t best = 0;
-                int bs1 = s2;
-                for (long long k = 2; k * s2 < 2LL * nt; k++) {
-                    const size_t n = need(s2, (int)(k * s2));
-                    if (!best || n < best) {
-                        best = n;
-                        bs1 = (int)(k * s2);
-                    }
-                }
-                if (best && best <= avail) {
-                    S_ = s2;
-                    So_ = bs1;
-                    break;
-                }
-            }
-            // nothing fits: keep one level, whose allocation below reports the shortfall
-        }
+        avail = fr > margin ? fr - margin : 0;
+    }
+    int So_ = S_;
+    {
+        size_t planned = 0;
+        st = behf_checkpoint_plan(nt, c->ck_stride, c->ck_outer, ck_bytes, snap_bytes, (size_t)c->nrec * nt * 8,
+                                  c->ck_outer > 0 ? (size_t)-1 : avail, &S_, &So_, &planned);
+        if (st) return st;
     }
     const int nseg = (nt + S_ - 1) / S_;      // snapshot segments (one level: also the checkpoint segments)
     const int nout = (nt + So_ - 1) / So_;      // outer segments (= nseg with one level)
