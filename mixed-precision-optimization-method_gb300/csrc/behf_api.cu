@@ -1270,49 +1270,51 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemcpy(d_adj, adj.data(), adj.size() * 8, cudaMemcpyHostToDevice));
 
     for (int og = nout - 1; og >= 0; og--) {
-      const int o0 = og * So_, o1 = std::min(nt, o0 + So_);
-      const int nin = two ? (o1 - o0 + S_ - 1) / S_ : 1;
-      if (two) {  // run the outer segment forward again from its checkpoint, keeping a checkpoint every S_ steps
-          CK(copy_state(ck + ck_bytes * og, false));
-          CK(cudaMemcpyAsync(c->d_it, &o0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-          CK(cudaStreamSynchronize(c->stream));
-          for (int j = 0; j < nin; j++) {
-              CK(copy_state(ckin + ck_bytes * j, true));
-              for (int it = o0 + j * S_; it < std::min(o1, o0 + (j + 1) * S_); it++) CK(snap_step(-1, -1, false));
-          }
-      }
-      for (int j = nin - 1; j >= 0; j--) {
-        const int sg = two ? -1 : og;  // the segment's index in the snapshot cache (never cached with two levels)
-        const int s0 = o0 + j * S_, s1 = std::min(o1, s0 + S_);
-        char* ckp = two ? ckin + ck_bytes * j : ck + ck_bytes * og;
-        if (!cached(sg)) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
-            CK(copy_state(ckp, false));
-            CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        const int o0 = og * So_, o1 = std::min(nt, o0 + So_);
+        const int nin = two ? (o1 - o0 + S_ - 1) / S_ : 1;
+        if (two) {  // run the outer segment forward again from its checkpoint, keeping a checkpoint every S_ steps
+            CK(copy_state(ck + ck_bytes * og, false));
+            CK(cudaMemcpyAsync(c->d_it, &o0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
             CK(cudaStreamSynchronize(c->stream));
-            CK(snap_fields(sg, 0));
-            for (int it = s0; it < s1; it++) CK(snap_step(sg, it - s0 + 1, false));
-        }
-        CK(build_snap_maps(sg));
-        // backward step it: T^T per cell of it is done (the first step: here, after its record^T; later steps: fused
-        // into the V^T gather of step it + 1, completed by the record^T of it)
-        for (int it = s1 - 1; it >= s0; it--) {
-            for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(sg, it - s0 + 1, f);
-            for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(sg, it - s0, BEHF_QX + d);
-            for (int d = 0; d < 6; d++) a.vq1[d] = snap_ptr(sg, it - s0, BEHF_VX + d);
-            if (it == nt - 1) {
-                CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
-                CK(adj_first<S>(g, c->p, a, c->stream));
-                c->launches += 2;
+            for (int j = 0; j < nin; j++) {
+                CK(copy_state(ckin + ck_bytes * j, true));
+                for (int it = o0 + j * S_; it < std::min(o1, o0 + (j + 1) * S_); it++) CK(snap_step(-1, -1, false));
             }
-            const int fuse = it >= 1 ? 1 : 0;
-            const bool sm = !snap_mt.empty();
-            CK(adj_step<S>(g, c->p, a, *maps, sm ? &snap_mt[it - s0 + 1] : nullptr, sm ? &snap_mv[it - s0] : nullptr,
-                           fuse, c->stream));
-            CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
-            if (fuse) CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc, c->stream));
-            c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
         }
-      }
+        for (int j = nin - 1; j >= 0; j--) {
+            const int sg = two ? -1 : og;  // the segment's index in the snapshot cache (never cached with two levels)
+            const int s0 = o0 + j * S_, s1 = std::min(o1, s0 + S_);
+            char* ckp = two ? ckin + ck_bytes * j : ck + ck_bytes * og;
+            if (!cached(sg)) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
+                CK(copy_state(ckp, false));
+                CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                CK(snap_fields(sg, 0));
+                for (int it = s0; it < s1; it++) CK(snap_step(sg, it - s0 + 1, false));
+            }
+            CK(build_snap_maps(sg));
+            // backward step it: T^T per cell of it is done (the first step: here, after its record^T; later steps:
+            // fused into the V^T gather of step it + 1, completed by the record^T of it)
+            for (int it = s1 - 1; it >= s0; it--) {
+                for (int f = 0; f < kNField; f++) a.cur[f] = snap_ptr(sg, it - s0 + 1, f);
+                for (int d = 0; d < 3; d++) a.qprev[d] = snap_ptr(sg, it - s0, BEHF_QX + d);
+                for (int d = 0; d < 6; d++) a.vq1[d] = snap_ptr(sg, it - s0, BEHF_VX + d);
+                if (it == nt - 1) {
+                    CK(adj_record<S>(a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it, sc, c->stream));
+                    CK(adj_first<S>(g, c->p, a, c->stream));
+                    c->launches += 2;
+                }
+                const int fuse = it >= 1 ? 1 : 0;
+                const bool sm = !snap_mt.empty();
+                CK(adj_step<S>(g, c->p, a, *maps, sm ? &snap_mt[it - s0 + 1] : nullptr,
+                               sm ? &snap_mv[it - s0] : nullptr, fuse, c->stream));
+                CK(adj_point<S>(a, so, c->src_kind, fac, c->d_wavelet, c->nw, it, d_gw, d_gfac, c->stream));
+                if (fuse)
+                    CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc,
+                                     c->stream));
+                c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
+            }
+        }
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     st = behf_sync(c);
