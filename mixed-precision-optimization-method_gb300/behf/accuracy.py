@@ -1,4 +1,5 @@
-"""Full-size accuracy of the storage precisions: seismogram relative L2 per recorded field.
+"""Full-size accuracy of the storage precisions: seismogram relative L2 per recorded field and, except at 1024^3,
+the relative L2 of each of the 13 final wavefields.
 
     python -m behf.accuracy --workload layered256 [--steps 2000]
         FP64 (the plain kernels, the GPU oracle run of the same scheme) vs FP32, FP16, BF16 (tiled kernels)
@@ -6,9 +7,10 @@
         FP16 and BF16 vs FP32 (FP64 at 1024^3 does not fit one GPU; FP32 is within 1e-4 of FP64 on the
         parity tests, so the FP16-vs-FP32 error stands for FP16-vs-FP64)
 
-Prints one JSON object: per precision and per recorded field the relative L2 error of all traces, the
-storage scales, the wall time, and the health check (NaN/Inf/saturation) at the end.  Runs the precisions
-one after another (one context on the device at a time).
+Prints one JSON object: per precision and per recorded field the relative L2 error of all traces, per
+wavefield the relative L2 error of the final field (physical units, read back as float32; skipped at 1024^3,
+where 13 fields are 56 GB of host memory per run), the storage scales, the wall time, and the health check
+(NaN/Inf/saturation) at the end.  Runs the precisions one after another (one context on the device at a time).
 """
 from __future__ import annotations
 
@@ -23,7 +25,7 @@ from . import problems
 
 
 def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0, state_rounding: int = 0,
-            scale_boost: int = 0):
+            scale_boost: int = 0, fields: bool = False):
     half = precision in ("f16", "bf16")
     scales = None
     if scale_boost and half:  # the automatic scales times 2^scale_boost
@@ -38,9 +40,10 @@ def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0, 
     seis = s.seismograms()
     ok, _ = s.health()
     info = s.info()
+    final = {name: s.get_field(name) for name in FIELDS} if fields else None
     s.close()
     return seis, {"wall_s": wall, "health_ok": bool(ok), "kernel": info["kernel"], "scales": info["scales"],
-                  "gpts": prob.cells * prob.nt / wall / 1e9}
+                  "gpts": prob.cells * prob.nt / wall / 1e9}, final
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
@@ -56,6 +59,7 @@ def main(argv=None):
     ap.add_argument("--coef-rounding", type=int, default=0, help="1: unbiased coefficient rounding (16-bit kinds)")
     ap.add_argument("--state-rounding", type=int, default=0, help="1: stochastic rounding of the stored fields")
     ap.add_argument("--scale-boost", type=int, default=0, help="16-bit kinds: automatic scales times 2^B")
+    ap.add_argument("--no-fields", action="store_true", help="skip the final-wavefield errors")
     args = ap.parse_args(argv)
     if args.workload == "layered256":
         prob = problems.layered256(n=args.n or 256, nt=args.steps or 2000)
@@ -69,14 +73,17 @@ def main(argv=None):
     out = {"workload": prob.name, "cells": prob.cells, "steps": prob.nt, "reference": ref_prec, "runs": {},
            "coef_rounding": args.coef_rounding, "state_rounding": args.state_rounding,
            "scale_boost": args.scale_boost}
-    ref, meta = run_one(prob, ref_prec)
+    fields = not args.no_fields and args.workload != "random1024"
+    ref, meta, ref_fields = run_one(prob, ref_prec, fields=fields)
     out["runs"][ref_prec] = meta
     comps = np.unique(prob.rec_comp)
     out["peak"] = {FIELDS[c]: float(np.abs(ref[prob.rec_comp == c]).max()) for c in comps}
     for prec in others:
-        seis, meta = run_one(prob, prec, coef_rounding=args.coef_rounding, state_rounding=args.state_rounding,
-                             scale_boost=args.scale_boost)
+        seis, meta, final = run_one(prob, prec, coef_rounding=args.coef_rounding,
+                                    state_rounding=args.state_rounding, scale_boost=args.scale_boost, fields=fields)
         meta["rel_l2"] = {FIELDS[c]: rel_l2(seis[prob.rec_comp == c], ref[prob.rec_comp == c]) for c in comps}
+        if fields:
+            meta["field_rel_l2"] = {name: rel_l2(final[name], ref_fields[name]) for name in FIELDS}
         out["runs"][prec] = meta
     print(json.dumps(out))
     return out

@@ -285,3 +285,18 @@ def test_stochastic_rounding_options(behf_lib, oracle, precision):
     assert max(errs.values()) < TOL[precision], errs
     np.testing.assert_array_equal(runs[0], runs[1])
     assert not np.array_equal(runs[0], runs[2])
+
+
+def test_accuracy_report_small(behf_lib):
+    """behf.accuracy on a 32^3, 60-step case: seismogram and final-wavefield relative L2 of every storage kind
+    against the GPU FP64 run (the CPU FP16/BF16 emulation gives 1.5e-3 / 2.2e-2 for the fields here)."""
+    import behf
+    from behf import accuracy
+
+    out = accuracy.main(["--workload", "small64", "--n", "32", "--steps", "60"])
+    for prec, tol in (("f32", 1e-4), ("f16", 1e-2), ("bf16", 0.1)):
+        run = out["runs"][prec]
+        assert run["health_ok"]
+        assert max(run["rel_l2"].values()) < tol, (prec, run["rel_l2"])
+        assert sorted(run["field_rel_l2"]) == sorted(behf.FIELDS)
+        assert max(run["field_rel_l2"].values()) < tol, (prec, run["field_rel_l2"])
