@@ -13,6 +13,9 @@
 // of the field it multiplies times the forward factor it multiplies (the forward states come from
 // sqrt(N)-style checkpoints: the segment is recomputed and its post-V states kept).
 //
+// orc_adjoint_ex can also round the 13 adjoint fields to binary16 times per-field scales between steps (an
+// FP16-stored adjoint state) and report their peak magnitudes: the measure of what such storage would cost.
+//
 // Gradient domain: coefficients of cells outside every CPML slab and inside the updated region are
 // differentiated; moduli gradients are exact for cells whose coefficient cells (c - {0,1}^3) all lie
 // in that domain, and set to zero elsewhere (the absorbing layers are not inverted).
@@ -438,9 +441,10 @@ struct Adj {
 
 }  // namespace
 
-extern "C" int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
-                           int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
-                           double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod) {
+extern "C" int orc_adjoint_ex(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
+                              int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
+                              double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod,
+                              const double* lf_scale, double* lf_max, long long* lf_saturated) {
     if (!cfg || cfg->radius < 1 || cfg->radius > 4 || nt < 1) return -1;
     Adj A;
     A.nx = cfg->nx;
@@ -606,6 +610,24 @@ extern "C" int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD],
             if (cfg->src_kind == ORC_SRC_EXPLOSIVE) gw = A.lf[ORC_SXX][so] + A.lf[ORC_SYY][so] + A.lf[ORC_SZZ][so];
             else if (cfg->src_kind == ORC_SRC_PRESSURE) gw = A.lf[ORC_P][so];
             if (grad_wavelet) grad_wavelet[it] = gw;
+            // adjoint-state storage: the largest magnitude of each adjoint field, and optionally the state
+            // rounded to binary16 times a per-field scale between steps (what an FP16-stored adjoint keeps)
+            for (int q = 0; q < ORC_NFIELD && (lf_max || lf_scale); q++) {
+                double mx = lf_max ? lf_max[q] : 0.0;
+                long long sat = 0;
+                const double sc = lf_scale ? lf_scale[q] : 0.0;
+                for (size_t c = 0; c < N; c++) {
+                    double& v = A.lf[q][c];
+                    mx = std::max(mx, std::fabs(v));
+                    if (sc > 0) {
+                        const double w = (double)(_Float16)(v * sc);
+                        if (std::isinf(w)) sat++;
+                        v = w / sc;
+                    }
+                }
+                if (lf_max) lf_max[q] = mx;
+                if (lf_saturated) *lf_saturated += sat;
+            }
         }
     }
 
@@ -706,4 +728,11 @@ extern "C" int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD],
                 for (int q = 0; q < ORC_NMOD; q++) grad_mod[(size_t)q * N + c] = in ? GM(q, c) : 0.0;
             }
     return 0;
+}
+
+extern "C" int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
+                           int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
+                           double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod) {
+    return orc_adjoint_ex(cfg, mod, wavelet, nt, nrec, rec_ijk, rec_comp, adj_src, stride, seis_out, grad_wavelet,
+                          grad_coef, grad_mod, nullptr, nullptr, nullptr);
 }

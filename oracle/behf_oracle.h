@@ -99,6 +99,15 @@ int orc_adjoint(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const floa
                 int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
                 double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod);
 
+/* orc_adjoint with adjoint-state storage emulation: lf_scale[13] (NULL = none) rounds each adjoint field to
+ * binary16 times lf_scale[q] after every backward step (an FP16-stored adjoint state; CPML adjoint memory and
+ * the gradients stay FP64); lf_max[13] (NULL = none; accumulated into, so zero it first) receives the largest
+ * magnitude of each adjoint field over the steps; lf_saturated (NULL = none) counts values that overflowed. */
+int orc_adjoint_ex(const orc_cfg* cfg, const float* const mod[ORC_NMOD], const float* wavelet, int nt,
+                   int nrec, const int* rec_ijk, const int* rec_comp, const double* adj_src, int stride,
+                   double* seis_out, double* grad_wavelet, double* grad_coef, double* grad_mod,
+                   const double* lf_scale, double* lf_max, long long* lf_saturated);
+
 /* Wall seconds of the time-step loop of the last orc_run (set-up excluded); OpenMP thread count. */
 double orc_last_step_seconds(void);
 int orc_threads(void);

@@ -167,11 +167,13 @@ def _cfg(prob, precision="f64", nthreads=0):
 
 
 def adjoint(prob, adj_src=None, stride: int = 0, nt: int | None = None, want_coef: bool = False,
-            mod=None, nthreads: int = 0):
+            mod=None, nthreads: int = 0, lf_scale=None):
     """FP64 discrete adjoint (behf_adjoint.cpp) of a problem description, physical units.
 
-    adj_src [nrec, nt]: dJ/d seismogram sample (None: zero).  mod overrides prob.mod.
-    Returns dict(seis [nrec, nt], grad_wavelet [nt], grad_mod [9, nz, ny, nx], grad_coef [23, ...] or None)."""
+    adj_src [nrec, nt]: dJ/d seismogram sample (None: zero).  mod overrides prob.mod.  lf_scale [13]: store the
+    adjoint state as binary16 times these per-field scales between steps (None: FP64).
+    Returns dict(seis [nrec, nt], grad_wavelet [nt], grad_mod [9, nz, ny, nx], grad_coef [23, ...] or None,
+    lf_max [13] (largest magnitude of each adjoint field), lf_saturated (values that overflowed binary16))."""
     nt = prob.nt if nt is None else nt
     cfg = _cfg(prob, "f64", nthreads)
     mod = _c(prob.mod if mod is None else mod, np.float32)
@@ -185,13 +187,17 @@ def adjoint(prob, adj_src=None, stride: int = 0, nt: int | None = None, want_coe
     gmod = np.zeros((NMOD, prob.nz, prob.ny, prob.nx), np.float64)
     gcoef = np.zeros((NCOEF, prob.nz, prob.ny, prob.nx), np.float64) if want_coef else None
     D = lambda a: a.ctypes.data_as(_P(C.c_double)) if a is not None else None  # noqa: E731
-    lib().orc_adjoint.restype = C.c_int
-    rcode = lib().orc_adjoint(C.byref(cfg), _ptrs(list(mod), C.c_float), w.ctypes.data_as(_P(C.c_float)), nt, nrec,
-                              ri.ctypes.data_as(_P(C.c_int)), rc.ctypes.data_as(_P(C.c_int)), D(adj), int(stride),
-                              D(seis), D(gw), D(gcoef), D(gmod))
+    scale = None if lf_scale is None else _c(lf_scale, np.float64)
+    lf_max = np.zeros(NFIELD, np.float64)
+    sat = C.c_longlong(0)
+    lib().orc_adjoint_ex.restype = C.c_int
+    rcode = lib().orc_adjoint_ex(C.byref(cfg), _ptrs(list(mod), C.c_float), w.ctypes.data_as(_P(C.c_float)), nt,
+                                 nrec, ri.ctypes.data_as(_P(C.c_int)), rc.ctypes.data_as(_P(C.c_int)), D(adj),
+                                 int(stride), D(seis), D(gw), D(gcoef), D(gmod), D(scale), D(lf_max), C.byref(sat))
     if rcode != 0:
         raise ValueError(f"orc_adjoint failed with {rcode}")
-    return {"seis": seis, "grad_wavelet": gw, "grad_mod": gmod, "grad_coef": gcoef}
+    return {"seis": seis, "grad_wavelet": gw, "grad_mod": gmod, "grad_coef": gcoef, "lf_max": lf_max,
+            "lf_saturated": int(sat.value)}
 
 
 def last_step_seconds() -> float:

@@ -79,3 +79,25 @@ def test_adjoint_gradient_vs_finite_differences(oracle, kind, R, L):
         fd = J(mp)[0] - J(mm)[0]
         pred = float((g[q] * (mp[q].astype(np.float64) - mm[q].astype(np.float64))).sum())
         assert abs(fd - pred) <= 1e-3 * abs(fd), (MODULI[q], fd, pred)
+
+
+def test_adjoint_state_storage_emulation(oracle):
+    """The FP16 adjoint-state emulation (lf_scale): no scale leaves the FP64 result unchanged; per-field scales
+    that put each adjoint field's peak just below 2^14 keep the gradients of this short case within 1e-2 without
+    overflow; a scale far too large overflows binary16 and is counted."""
+    p = small(R=2, L=4)
+    r = np.random.default_rng(3).standard_normal((len(p.rec_comp), p.nt))
+    ref = oracle.adjoint(p, r)
+    again = oracle.adjoint(p, r, lf_scale=None)
+    np.testing.assert_array_equal(ref["grad_mod"], again["grad_mod"])
+    mx = ref["lf_max"]
+    assert mx.shape == (13,) and (mx > 0).all() and ref["lf_saturated"] == 0
+    scale = 2.0 ** np.floor(np.log2(2.0 ** 14 / mx))
+    emu = oracle.adjoint(p, r, lf_scale=scale)
+    assert emu["lf_saturated"] == 0
+    for q in range(9):
+        d = np.linalg.norm(ref["grad_mod"][q])
+        assert np.linalg.norm(emu["grad_mod"][q] - ref["grad_mod"][q]) <= 1e-2 * d, MODULI[q]
+    assert not np.array_equal(emu["grad_mod"], ref["grad_mod"])  # the rounding did happen
+    over = oracle.adjoint(p, r, lf_scale=scale * 2.0 ** 8)
+    assert over["lf_saturated"] > 0
