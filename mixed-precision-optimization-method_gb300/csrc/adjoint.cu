@@ -1033,13 +1033,7 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
                   const GatherMaps* snapV, int fuse, cudaStream_t st) {
     const dim3 block(32, 8, 1);
     const int nxu = g.nx - 2 * R, nyu = g.ny - 2 * R, nzu = g.nz - 2 * R;
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 148;
-    }
+    const int sms = device_sms();
     // z chunks that fill the last wave of resident CTAs, at most 64 planes, at least BEHF_ADJ_MINW waves (measured
     // at 192^3 with the fused gathers: 2 waves of 46-plane chunks 553 + 615 us per step, 5 waves of 17 planes
     // 499 + 516 us)
@@ -1062,8 +1056,9 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
     constexpr bool split = BEHF_ADJ_SPLIT != 0;
     constexpr int MG = split ? 1 : 0;  // the gathers' mode
     const int smemg = GMap<S, R, MG>::BYTES + 128, smemd = GMap<S, R, 2>::BYTES + 128;
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag flag;
+    static cudaError_t status = cudaSuccess;
+    const cudaError_t ea = run_once(flag, status, [&] {
         cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_gather<S, R, 1, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);
@@ -1071,9 +1066,9 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
             e = cudaFuncSetAttribute(k_gather<S, R, 0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemd);
         if (e == cudaSuccess && split)
             e = cudaFuncSetAttribute(k_gather<S, R, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemd);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+        return e;
+    });
+    if (ea != cudaSuccess) return ea;
     if ((split || GMap<S, R, 0>::SNAP) && a.grad && (!snapT || (fuse && !snapV))) return cudaErrorInvalidValue;
     // T^T gather + V^T; its V-coefficient gradients; V^T gather + T-slot memory + T^T of step n - 1; its
     // T-coefficient gradients

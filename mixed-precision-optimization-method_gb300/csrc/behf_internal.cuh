@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "behf.h"
 
@@ -115,6 +116,25 @@ struct Geom {
 
 __host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
     return i < L ? i : (i >= n - 1 - L ? L + (i - (n - 1 - L)) : -1);
+}
+
+// SMs of the current device, read once per process (thread-safe initialisation; 148 if the query fails).
+inline int device_sms() {
+    static const int n = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return sms > 0 ? sms : 148;
+    }();
+    return n;
+}
+
+// Runs f once per process for the flag's owner (a kernel's shared-memory opt-in), also when several host threads
+// launch at the same time; every caller gets f's status.
+template <class F>
+inline cudaError_t run_once(std::once_flag& flag, cudaError_t& status, F&& f) {
+    std::call_once(flag, [&] { status = f(); });
+    return status;
 }
 
 // z planes per CTA of a z-marching launch over nxy tiles and `planes` planes with `slots` CTAs resident per

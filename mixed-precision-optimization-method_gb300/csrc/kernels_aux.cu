@@ -263,14 +263,7 @@ __global__ void k_set(void* f, const float* in, int nx, int ny, int nz, long lon
 }  // namespace
 
 int aux_grid_blocks() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        n = (sms > 0 ? sms : 132) * 8;
-    }
-    return n;
+    return device_sms() * 8;
 }
 
 template <class S>

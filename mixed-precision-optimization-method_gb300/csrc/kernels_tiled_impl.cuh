@@ -623,17 +623,6 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     return ok;
 }
 
-inline int num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 148;
-    }
-    return n;
-}
-
 template <class S, int R>
 cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) {
     const int nbx = (g.nx - R + TXC - 1) / TXC, nby = (g.ny - R + TY - 1) / TY;
@@ -644,27 +633,27 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // that, a chunk count that fills the last wave of resident CTAs (MINB per SM) with at least four waves where
     // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
     // for two waves of 36-plane chunks)
-    const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * num_sms();
+    const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * device_sms();
     int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, BEHF_TILED_MINW);
     if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
     if (vel) {
         const int smem = Map<S, R, true>::bytes + 128;
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_vel<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
+        static std::once_flag flag;
+        static cudaError_t status = cudaSuccess;
+        const cudaError_t e = run_once(flag, status, [&] {
+            return cudaFuncSetAttribute(k_vel<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        });
+        if (e != cudaSuccess) return e;
         k_vel<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const VMaps*>(maps), g, p, zchunk);
     } else {
         const int smem = Map<S, R, false>::bytes + 128;
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(k_str<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
+        static std::once_flag flag;
+        static cudaError_t status = cudaSuccess;
+        const cudaError_t e = run_once(flag, status, [&] {
+            return cudaFuncSetAttribute(k_str<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        });
+        if (e != cudaSuccess) return e;
         k_str<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const TMaps*>(maps), g, p, zchunk);
     }
     return cudaGetLastError();
