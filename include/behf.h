@@ -11,7 +11,9 @@
  * This header splits that boundary into setup, run and output calls over an opaque context.
  * Every call returns a behf_status and never exits the process (the reference's CUDA_CHECK calls
  * exit(), kernel.cu:42-52).  A context is single-thread affine and owns one CUDA stream; separate
- * contexts may be driven from separate threads.  All host pointers are copied; the caller keeps
+ * contexts may be driven from separate threads.  A context lives on the device that was current
+ * when it was created: each call on it makes that device current for the call and restores the
+ * caller's device afterwards, so contexts on several GPUs can be driven from one process.  All host pointers are copied; the caller keeps
  * ownership.  Arrays are C order [nz][ny][nx] (x fastest), as the reference's
  * offset = ix + iy*nxt + iz*nxt*nyt (kernel.cu:162).
  */
@@ -106,6 +108,9 @@ enum {
     BEHF_OPT_CHECKPOINT_OUTER = 9, /* gradient: outer checkpoint spacing of the two-level scheme, rounded up to a
                                     multiple of BEHF_OPT_CHECKPOINT (0 = automatic: one level when it fits the
                                     device memory, else two levels with the inner spacing halved until they fit) */
+    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic, 1 = classic (own-cell data by direct loads of the
+                                    compute threads), 2 = warp-specialised (a producer warp brings every input,
+                                    own-cell data included, through TMA) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current
@@ -192,7 +197,8 @@ behf_status behf_get_stream(behf_ctx* ctx, void** stream);
 
 /* Health check (energy-norm reduction in FP64 over every field, on the device): writes the sum of
  * squares of each field in storage units to norms[BEHF_NFIELD] and returns BEHF_ERR_NONFINITE if any
- * value is NaN/Inf or saturates the storage format.  The reference has no counterpart (it prints
+ * value is NaN/Inf or saturates the storage format (reaches its largest finite value: 65504 for FP16,
+ * (2 - 2^-7) 2^127 for BF16); flagged values are left out of the sums.  The reference has no counterpart (it prints
  * or ignores errors, kernel.cu:1926-1929). */
 behf_status behf_health(behf_ctx* ctx, double* norms);
 
@@ -201,8 +207,10 @@ behf_status behf_health(behf_ctx* ctx, double* norms);
  * memory through its own pool (nothing left for cudaMalloc), or a monitoring thread that checks a
  * running simulation and must not stall the device with cudaFree.
  *   field      device array of `precision` values laid out [nz][ny][pitch] with plane stride `plane`
- *   norm_out   device double: sum of squares of the nx*ny*nz values (the storage units of the field)
- *   flag_out   device int: 1 if any value is NaN/Inf or at the top of the storage range, else 0
+ *   norm_out   device double: sum of squares of the nx*ny*nz values (the storage units of the field); values
+ *              that set the flag are left out of it, as behf_health leaves them out
+ *   flag_out   device int: 1 if any value is NaN/Inf or at the top of the storage range (65504 for FP16,
+ *              (2 - 2^-7) 2^127 for BF16, FLT_MAX / DBL_MAX for FP32 / FP64), else 0
  *   stream     cudaStream_t to run on (NULL: the default stream); the call does not synchronize
  * Fields up to 2^30 cells (1024^3); larger sizes are rejected with BEHF_ERR_INVALID.  Scratch is a
  * fixed 512 KiB device array inside the library, held by every GPU that loads it until exit.  The
@@ -228,6 +236,25 @@ behf_status behf_gradient(behf_ctx* ctx, int nt, const double* adj_src, double* 
  * adjoint source is the residual of the forward pass; J is written to *misfit. */
 behf_status behf_misfit_gradient(behf_ctx* ctx, int nt, const double* observed, double* misfit,
                                  double* grad_wavelet, double* const grad_moduli[BEHF_NMOD]);
+
+/* Biot's physical parameters of behf_physical_gradient: the drained Lame parameter lambda, the shear modulus mu,
+ * the bulk density rho, the fluid density rho_f, the Biot modulus M, the Biot coefficient alpha and the
+ * permeability kappa. */
+enum { BEHF_PH_LAMBDA = 0, BEHF_PH_MU, BEHF_PH_RHO, BEHF_PH_RHOF, BEHF_PH_M, BEHF_PH_ALPHA, BEHF_PH_KAPPA, BEHF_NPHYS };
+
+/* Chain rule from the moduli gradients of behf_gradient / behf_misfit_gradient to the physical parameters (no
+ * counterpart in the reference, which has no adjoint).  Host arithmetic only, cell by cell over ncell cells.
+ * The moduli relate to the parameters as the reference's create_model_all builds them (outputfunc.cpp:202-217):
+ * C = alpha M, lambda_u = lambda + alpha^2 M, H = lambda_u + 2 mu, b = eta / kappa, m = (m / rho_f) rho_f, with eta
+ * and m / rho_f = (1 + 2/8) tau / phi held fixed per cell.
+ *   moduli        BEHF_NMOD host arrays [ncell] float (the medium passed to behf_set_medium); rho_f, M, C, b, m
+ *                 are required
+ *   grad_moduli   BEHF_NMOD host arrays [ncell] double (NULL entries count as zero)
+ *   eta           fluid viscosity (Pa s; the reference's 1e-3, outputfunc.cpp:166)
+ *   grad_phys     BEHF_NPHYS host arrays [ncell] double, dJ / d parameter (NULL entries are skipped) */
+behf_status behf_physical_gradient(long long ncell, const float* const moduli[BEHF_NMOD],
+                                   const double* const grad_moduli[BEHF_NMOD], double eta,
+                                   double* const grad_phys[BEHF_NPHYS]);
 
 /* Autotuner (no counterpart in the reference): times trial_steps steps for each z-chunk length of the tiled
  * kernels (BEHF_OPT_ZCHUNK candidates 0, 16, 32, ... up to the grid), keeps the fastest, and resets the

@@ -19,11 +19,13 @@ _lib = None
 FIELDS = ["vx", "vy", "vz", "qx", "qy", "qz", "sxx", "syy", "szz", "sxy", "sxz", "syz", "p"]
 FIELD = {n: i for i, n in enumerate(FIELDS)}
 MODULI = ["rho", "rhof", "mu", "M", "C", "HH", "H2u", "C1", "C2"]
+PHYSICAL = ["lambda", "mu", "rho", "rhof", "M", "alpha", "kappa"]
 PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
 (OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
- OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER) = range(10)
+ OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER, OPT_TILED_VARIANT) = range(11)
+TILED_VARIANT = {"auto": 0, "classic": 1, "ws": 2}
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -124,6 +126,7 @@ def load() -> C.CDLL:
                                  P(C.c_int), P(C.c_int), P(C.c_size_t)],
         "behf_field_norm_noalloc": [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
                                     C.c_void_p, C.c_void_p, C.c_void_p],
+        "behf_physical_gradient": [C.c_longlong, P(P(C.c_float)), P(P(C.c_double)), C.c_double, P(P(C.c_double))],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -350,6 +353,22 @@ def field_norm_noalloc(field_ptr: int, precision: str, nx: int, ny: int, nz: int
                                           C.c_void_p(norm_ptr), C.c_void_p(flag_ptr), C.c_void_p(stream)))
 
 
+def physical_gradient(mod: np.ndarray, grad_mod: np.ndarray, eta: float = 1e-3) -> np.ndarray:
+    """behf_physical_gradient (host, no GPU): dJ/d(lambda, mu, rho, rho_f, M, alpha, kappa) [7, ...] from the
+    moduli [9, ...] of the medium and the moduli gradient [9, ...] of Solver.gradient / misfit_gradient."""
+    mod = np.ascontiguousarray(mod, dtype=np.float32)
+    gm = np.ascontiguousarray(grad_mod, dtype=np.float64)
+    if mod.shape[0] != 9 or gm.shape != mod.shape:
+        raise ValueError("moduli and their gradient must both be [9, ...] of one shape")
+    n = int(np.prod(mod.shape[1:]))
+    out = np.zeros((7, *mod.shape[1:]), np.float64)
+    mp = (C.POINTER(C.c_float) * 9)(*[mod[q].ctypes.data_as(C.POINTER(C.c_float)) for q in range(9)])
+    gp = (C.POINTER(C.c_double) * 9)(*[gm[q].ctypes.data_as(C.POINTER(C.c_double)) for q in range(9)])
+    op = (C.POINTER(C.c_double) * 7)(*[out[q].ctypes.data_as(C.POINTER(C.c_double)) for q in range(7)])
+    _check(load().behf_physical_gradient(n, mp, gp, float(eta), op))
+    return out
+
+
 def algorithmic_bytes(precision: str, shape, cpml_width: int) -> dict:
     """Compulsory HBM bytes per cell update of each kernel and of a whole step.
 
@@ -414,5 +433,5 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
     return s
 
 
-__all__ = ["Solver", "BehfError", "solver_for", "run_batch", "checkpoint_plan", "load", "lib_path", "FIELDS", "FIELD",
-           "MODULI"]
+__all__ = ["Solver", "BehfError", "solver_for", "run_batch", "checkpoint_plan", "physical_gradient", "load", "lib_path",
+           "FIELDS", "FIELD", "MODULI", "PHYSICAL"]

@@ -57,6 +57,29 @@ def rock_moduli(Ks, Kf, Kdry, mu, rhos, rhof, phi, kappa, eta, tau):
     return out
 
 
+def physical_from_moduli(mod: np.ndarray, eta: float = 1e-3) -> tuple[np.ndarray, np.ndarray]:
+    """Biot's physical parameters [7, ...] (lambda, mu, rho, rho_f, M, alpha, kappa) of cell-centred moduli, and the
+    per-cell ratio m / rho_f = (1 + 2/8) tau / phi that they leave fixed (the inverse of moduli_from_physical).
+    Pure-fluid cells (b = 0) get kappa = inf."""
+    m = np.asarray(mod, np.float64)
+    rho, rhof, mu, M, Cc, HH, H2u, b, mm = m
+    alpha = np.divide(Cc, M, out=np.zeros_like(M), where=M != 0)
+    lam = H2u - alpha * alpha * M
+    with np.errstate(divide="ignore"):
+        kappa = np.where(b > 0, eta / np.where(b > 0, b, 1.0), np.inf)
+    ratio = np.divide(mm, rhof, out=np.zeros_like(mm), where=rhof != 0)
+    return np.stack([lam, mu, rho, rhof, M, alpha, kappa]), ratio
+
+
+def moduli_from_physical(phys: np.ndarray, m_over_rhof: np.ndarray, eta: float = 1e-3) -> np.ndarray:
+    """Cell-centred moduli [9, ...] float32 from physical parameters [7, ...]: C = alpha M, lambda_u = lambda +
+    alpha^2 M, H = lambda_u + 2 mu, b = eta / kappa, m = (m / rho_f) rho_f (outputfunc.cpp:202-217)."""
+    lam, mu, rho, rhof, M, alpha, kappa = np.asarray(phys, np.float64)
+    h2u = lam + alpha * alpha * M
+    b = np.where(np.isfinite(kappa), eta / kappa, 0.0)
+    return np.stack([rho, rhof, mu, M, alpha * M, h2u + 2 * mu, h2u, b, m_over_rhof * rhof]).astype(np.float32)
+
+
 def p_velocity(rock: dict) -> float:
     m = rock_moduli(**rock)
     return float(np.sqrt(m[5] / m[0]))

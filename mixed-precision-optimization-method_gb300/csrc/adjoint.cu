@@ -1056,9 +1056,8 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
     constexpr bool split = BEHF_ADJ_SPLIT != 0;
     constexpr int MG = split ? 1 : 0;  // the gathers' mode
     const int smemg = GMap<S, R, MG>::BYTES + 128, smemd = GMap<S, R, 2>::BYTES + 128;
-    static std::once_flag flag;
-    static cudaError_t status = cudaSuccess;
-    const cudaError_t ea = run_once(flag, status, [&] {
+    static PerDevice once;
+    const cudaError_t ea = run_once(once, [&] {
         cudaError_t e = cudaFuncSetAttribute(k_gather<S, R, 0, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_gather<S, R, 1, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemg);

@@ -502,6 +502,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.plane = g.px * gr->ny;
     g.bug = 0;
     g.zchunk_req = 0;
+    g.ws = 0;
     g.sr = 0;
     g.step = nullptr;
     g.step_off = 0;
@@ -583,6 +584,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
 
 behf_status behf_destroy(behf_ctx* c) {
     if (!c) return BEHF_OK;
+    DeviceScope device_scope(c->dev);
     cudaStreamSynchronize(c->stream);
     delete c;
     return BEHF_OK;
@@ -590,6 +592,7 @@ behf_status behf_destroy(behf_ctx* c) {
 
 behf_status behf_set_medium_device(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
     if (!c || !mod) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     for (int q = 0; q < kNMod; q++)
         if (!mod[q]) return fail(BEHF_ERR_INVALID, "modulus array %d is null", q);
     return set_medium_dev(c, mod);
@@ -597,6 +600,7 @@ behf_status behf_set_medium_device(behf_ctx* c, const float* const mod[BEHF_NMOD
 
 behf_status behf_set_medium(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
     if (!c || !mod) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
     float* dm[kNMod] = {};
     behf_status st = BEHF_OK;
@@ -617,6 +621,7 @@ behf_status behf_set_medium(behf_ctx* c, const float* const mod[BEHF_NMOD]) {
 
 behf_status behf_generate_medium(behf_ctx* c, const behf_medium_spec* spec) {
     if (!c || !spec) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     if (spec->nlayers < 1 || spec->nlayers > 4) return fail(BEHF_ERR_INVALID, "nlayers must be 1..4");
     const bool noise = spec->pct != 0 || spec->log_kappa_sigma != 0;
     if (noise && !(spec->corr_cells > 0)) return fail(BEHF_ERR_INVALID, "corr_cells must be positive");
@@ -641,6 +646,7 @@ behf_status behf_generate_medium(behf_ctx* c, const behf_medium_spec* spec) {
 
 behf_status behf_set_cpml_profile(behf_ctx* c, int axis, const double* d, const double* d2) {
     if (!c || axis < 0 || axis > 2 || !d || !d2) return fail(BEHF_ERR_INVALID, "bad argument");
+    DeviceScope device_scope(c->dev);
     const int n = axis == 0 ? c->grid.nx : axis == 1 ? c->grid.ny : c->grid.nz;
     c->prof_d[axis].assign(d, d + n);
     c->prof_d2[axis].assign(d2, d2 + n);
@@ -650,6 +656,7 @@ behf_status behf_set_cpml_profile(behf_ctx* c, int axis, const double* d, const 
 
 behf_status behf_set_source(behf_ctx* c, int kind, int ix, int iy, int iz, const float* w, int nt) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     if (kind < BEHF_SRC_EXPLOSIVE || kind > BEHF_SRC_FORCE_Z) return fail(BEHF_ERR_INVALID, "bad source kind %d", kind);
     const int R = c->g.R;
     const int ijk[3] = {ix, iy, iz}, n3[3] = {c->grid.nx, c->grid.ny, c->grid.nz};
@@ -675,6 +682,7 @@ behf_status behf_set_source(behf_ctx* c, int kind, int ix, int iy, int iz, const
 
 behf_status behf_set_receivers(behf_ctx* c, int nrec, const int* ijk, const int* comp, int capacity) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     if (nrec < 0 || capacity < 0 || (nrec > 0 && (!ijk || !comp)))
         return fail(BEHF_ERR_INVALID, "bad receiver arguments");
     std::vector<long long> off(nrec);
@@ -711,6 +719,7 @@ behf_status behf_set_receivers(behf_ctx* c, int nrec, const int* ijk, const int*
 
 behf_status behf_run_async(behf_ctx* c, int nsteps) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_run");
     if (nsteps < 0) return fail(BEHF_ERR_INVALID, "negative step count");
     if (c->nrec > 0 && c->step + nsteps > c->cap)
@@ -793,6 +802,7 @@ behf_status behf_checkpoint_plan(int nt, int checkpoint, int checkpoint_outer, s
 
 behf_status behf_sync(behf_ctx* c) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     CK(cudaStreamSynchronize(c->stream));
     int err = 0;
     CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -811,6 +821,7 @@ behf_status behf_run(behf_ctx* c, int nsteps) {
 
 behf_status behf_get_seismograms(behf_ctx* c, double* out, int* nrec_steps) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     const int ns = (int)(c->step < c->cap ? c->step : c->cap);
     if (nrec_steps) *nrec_steps = ns;
     if (!out || c->nrec == 0) return BEHF_OK;
@@ -826,6 +837,7 @@ behf_status behf_get_seismograms(behf_ctx* c, double* out, int* nrec_steps) {
 
 static behf_status field_io(behf_ctx* c, int q, float* host, bool get) {
     if (!c || !host) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     if (q < 0 || q >= kNField) return fail(BEHF_ERR_INVALID, "bad field %d", q);
     const size_t N = (size_t)c->grid.nx * c->grid.ny * c->grid.nz;
     float* tmp = nullptr;
@@ -860,11 +872,13 @@ behf_status behf_set_field(behf_ctx* c, int q, const float* in) { return field_i
 
 behf_status behf_reset(behf_ctx* c) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     return zero_state(c);
 }
 
 behf_status behf_set_option(behf_ctx* c, int opt, int value) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     switch (opt) {
         case BEHF_OPT_KERNEL:
             if (value < BEHF_KERNEL_AUTO || value > BEHF_KERNEL_TILED) return fail(BEHF_ERR_INVALID, "bad kernel %d", value);
@@ -907,6 +921,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative z chunk");
             c->g.zchunk_req = value;
             break;
+        case BEHF_OPT_TILED_VARIANT:
+            if (value < 0 || value > 2) return fail(BEHF_ERR_INVALID, "tiled variant must be 0, 1 or 2");
+            c->g.ws = value == 2 ? 1 : 0;
+            break;
         default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
     }
     c->invalidate_graph();
@@ -933,6 +951,7 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
 
 behf_status behf_update_wavelet(behf_ctx* c, int it0, const float* w, int n) {
     if (!c || (n > 0 && !w) || it0 < 0 || n < 0) return fail(BEHF_ERR_INVALID, "bad argument");
+    DeviceScope device_scope(c->dev);
     if (!c->src_set) return fail(BEHF_ERR_STATE, "behf_set_source must come first");
     if (it0 + n > c->nw) {  // grow, keeping the old samples
         float* nw = nullptr;
@@ -952,6 +971,7 @@ behf_status behf_update_wavelet(behf_ctx* c, int it0, const float* w, int n) {
 
 behf_status behf_get_seismograms_range(behf_ctx* c, int it0, int n, double* out) {
     if (!c || n < 0 || it0 < 0 || (n > 0 && !out)) return fail(BEHF_ERR_INVALID, "bad argument");
+    DeviceScope device_scope(c->dev);
     if (it0 + n > c->cap) return fail(BEHF_ERR_INVALID, "range beyond the receiver capacity %d", c->cap);
     if (c->nrec == 0 || n == 0) return BEHF_OK;
     CK(cudaMemcpy2DAsync(out, (size_t)n * 8, c->d_seis + it0, (size_t)c->cap * 8, (size_t)n * 8, c->nrec,
@@ -962,6 +982,7 @@ behf_status behf_get_seismograms_range(behf_ctx* c, int it0, int n, double* out)
 
 behf_status behf_time_kernels(behf_ctx* c, int nsteps, double* ms) {
     if (!c || !ms || nsteps <= 0) return fail(BEHF_ERR_INVALID, "bad argument");
+    DeviceScope device_scope(c->dev);
     if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before timing");
     if (c->nrec > 0 && c->step + nsteps > c->cap) return fail(BEHF_ERR_INVALID, "receiver capacity exceeded");
     const int maxl = 4 * nsteps;
@@ -998,7 +1019,8 @@ behf_status behf_get_stream(behf_ctx* c, void** s) {
 
 behf_status behf_health(behf_ctx* c, double* norms) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
-    const double limit = c->prec == BEHF_FP16 ? 65504.0 : c->prec == BEHF_FP64 ? 1.7976931348623157e308 : 3.4028234663852886e38;
+    DeviceScope device_scope(c->dev);
+    const double limit = storage_max(c->prec);
     const Geom& g = c->g;
     CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
     for (int q = 0; q < kNField; q++) {
@@ -1412,17 +1434,20 @@ extern "C" {
 behf_status behf_gradient(behf_ctx* c, int nt, const double* adj_src, double* grad_wavelet,
                           double* const grad_moduli[BEHF_NMOD]) {
     if (!c || !adj_src) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     return gradient_dispatch(c, nt, adj_src, nullptr, nullptr, grad_wavelet, grad_moduli);
 }
 
 behf_status behf_misfit_gradient(behf_ctx* c, int nt, const double* observed, double* misfit, double* grad_wavelet,
                                  double* const grad_moduli[BEHF_NMOD]) {
     if (!c || !observed) return fail(BEHF_ERR_INVALID, "null argument");
+    DeviceScope device_scope(c->dev);
     return gradient_dispatch(c, nt, nullptr, observed, misfit, grad_wavelet, grad_moduli);
 }
 
 behf_status behf_selftest_wait(behf_ctx* c) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     CK(aux_wait_selftest(c->d_err, c->stream));
     c->launches++;
     return behf_sync(c);
@@ -1430,6 +1455,7 @@ behf_status behf_selftest_wait(behf_ctx* c) {
 
 behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double* ms_out) {
     if (!c) return fail(BEHF_ERR_INVALID, "null context");
+    DeviceScope device_scope(c->dev);
     if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_autotune");
     if (trial_steps < 1) return fail(BEHF_ERR_INVALID, "trial_steps must be positive");
     const int planes = c->grid.nz - 2 * c->g.R;

@@ -75,6 +75,18 @@ template <> struct Traits<__nv_bfloat16> {
     static constexpr int prec = BEHF_BF16;
 };
 
+// Largest finite value of each storage format: the health checks flag a stored value whose magnitude reaches it
+// (saturated by a rounding that overflowed into it, or past it as Inf).  BF16 keeps FP32's exponent range but only
+// 8 significand bits, so its top is (2 - 2^-7) 2^127, below FLT_MAX.
+inline double storage_max(int precision) {
+    switch (precision) {
+        case BEHF_FP16: return 65504.0;
+        case BEHF_BF16: return 3.3895313892515355e38;
+        case BEHF_FP32: return 3.4028234663852886e38;
+        default: return 1.7976931348623157e308;
+    }
+}
+
 // Staggered first-derivative weights of order 2R: D(i+1/2) = sum_m w_m (f[i+m] - f[i-m+1]) / h.
 template <int R>
 __host__ __device__ constexpr double stencil_w(int m) {
@@ -103,6 +115,7 @@ struct Geom {
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out
     int zchunk_req;        // tiled kernels: z planes per CTA (0 = automatic)
+    int ws;                // tiled kernels: 1 = warp-specialised variant (every read through TMA), 0 = classic
     int sr;                // 16-bit kinds, tiled kernels: stochastic rounding of the stored fields
     const int* step;       // device step counter (seeds the stochastic rounding)
     int step_off;          // step offset of this launch within a graph chunk
@@ -118,24 +131,54 @@ __host__ __device__ __forceinline__ int slab_index(int i, int n, int L) {
     return i < L ? i : (i >= n - 1 - L ? L + (i - (n - 1 - L)) : -1);
 }
 
-// SMs of the current device, read once per process (thread-safe initialisation; 148 if the query fails).
-inline int device_sms() {
-    static const int n = [] {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        return sms > 0 ? sms : 148;
-    }();
-    return n;
+// Per-device state is kept in arrays indexed by the CUDA device ordinal (at most kMaxDevices devices).
+constexpr int kMaxDevices = 64;
+inline int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+    return dev;
 }
 
-// Runs f once per process for the flag's owner (a kernel's shared-memory opt-in), also when several host threads
-// launch at the same time; every caller gets f's status.
-template <class F>
-inline cudaError_t run_once(std::once_flag& flag, cudaError_t& status, F&& f) {
-    std::call_once(flag, [&] { status = f(); });
-    return status;
+// SMs of the current device, read once per device (thread-safe; 148 if the query fails).
+inline int device_sms() {
+    static std::once_flag once[kMaxDevices];
+    static int sms[kMaxDevices];
+    const int dev = current_device();
+    std::call_once(once[dev], [&] {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = n > 0 ? n : 148;
+    });
+    return sms[dev];
 }
+
+// A set-up step that must run once on every device a kernel is launched on (a kernel's shared-memory opt-in:
+// cudaFuncSetAttribute applies to the current device only).  run_once runs f once per device, with that device
+// current, also when several host threads launch at the same time; every caller gets f's status on its device.
+struct PerDevice {
+    std::once_flag flag[kMaxDevices];
+    cudaError_t status[kMaxDevices] = {};
+};
+template <class F>
+inline cudaError_t run_once(PerDevice& pd, F&& f) {
+    const int dev = current_device();
+    std::call_once(pd.flag[dev], [&] { pd.status[dev] = f(); });
+    return pd.status[dev];
+}
+
+// Makes a context's device current for the duration of an entry point and restores the caller's device after.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
 
 // z planes per CTA of a z-marching launch over nxy tiles and `planes` planes with `slots` CTAs resident per
 // wave: the chunk length in [minz, maxz] minimising (waves, rounded up) x (chunk + halo), so that the last wave

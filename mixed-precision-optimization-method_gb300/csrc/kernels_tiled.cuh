@@ -110,10 +110,14 @@ constexpr int al128(int b) { return (b + 127) & ~127; }
 struct VMaps {
     CUtensorMap halo[6];  // txx(X) tyy(Y) txy(XY) txz(X) tyz(Y) p(XY)
     CUtensorMap zlead[4]; // tzz txz tyz p: own-cell boxes for the z ring
+    // own-cell boxes of the warp-specialised kernel: vx vy vz qx qy qz, VW1 x y z (FP32), then VW3, VU1, VU2
+    // (x y z each)
+    CUtensorMap own[18];
 };
 struct TMaps {
     CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
     CUtensorMap zlead[4]; // vx vy vz qz: own-cell boxes for the z ring
+    CUtensorMap own[14];  // sxx syy szz sxy sxz syz p, then P1 P2 S1 S2 Sxy Sxz Syz
 };
 
 // ------------------------------------------------------------------------------------- PTX helpers

@@ -594,6 +594,14 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
     if (tid == 0) producer_drain<M>(pp);
 }
 
+}  // namespace tiled
+}  // namespace behf
+
+#include "kernels_tiled_ws.cuh"
+
+namespace behf {
+namespace tiled {
+
 // ----------------------------------------------------------------------------------------- host side
 template <class S, int R>
 bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
@@ -620,6 +628,21 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
     ok &= encode<S>(&tm->zlead[1], g, p.f[BEHF_VY], TXC, TY);
     ok &= encode<S>(&tm->zlead[2], g, p.f[BEHF_VZ], TXC, TY);
     ok &= encode<S>(&tm->zlead[3], g, p.f[BEHF_QZ], TXC, TY);
+    // own-cell boxes (warp-specialised kernels)
+    typedef typename Traits<S>::K K;
+    typedef typename Traits<S>::W Wt;
+    for (int a = 0; a < 3; a++) {
+        ok &= encode<S>(&vm->own[a], g, p.f[BEHF_VX + a], TXC, TY);
+        ok &= encode<S>(&vm->own[3 + a], g, p.f[BEHF_QX + a], TXC, TY);
+        ok &= encode<Wt>(&vm->own[6 + a], g, p.k[VW1X + a], TXC, TY);
+        ok &= encode<K>(&vm->own[9 + a], g, p.k[VW3X + a], TXC, TY);
+        ok &= encode<K>(&vm->own[12 + a], g, p.k[VU1X + a], TXC, TY);
+        ok &= encode<K>(&vm->own[15 + a], g, p.k[VU2X + a], TXC, TY);
+    }
+    for (int q = 0; q < 7; q++) {
+        ok &= encode<S>(&tm->own[q], g, p.f[BEHF_SXX + q], TXC, TY);
+        ok &= encode<K>(&tm->own[7 + q], g, p.k[q < 4 ? P1 + q : P1 + q + 1], TXC, TY);
+    }
     return ok;
 }
 
@@ -633,28 +656,41 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // that, a chunk count that fills the last wave of resident CTAs (MINB per SM) with at least four waves where
     // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
     // for two waves of 36-plane chunks)
-    const int slots = (vel ? Depth<S>::MINB : Depth<S>::MINB_T) * device_sms();
+    const bool ws = g.ws != 0;
+    const int minb = ws ? WDepth<S>::MINB : vel ? Depth<S>::MINB : Depth<S>::MINB_T;
+    const int slots = minb * device_sms();
     int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, BEHF_TILED_MINW);
     if (g.zchunk_req > 0) zchunk = g.zchunk_req < planes ? g.zchunk_req : planes;
     const dim3 grid(nbx, nby, (planes + zchunk - 1) / zchunk);
-    if (vel) {
+    const VMaps& vm = *reinterpret_cast<const VMaps*>(maps);
+    const TMaps& tm = *reinterpret_cast<const TMaps*>(maps);
+    // each kernel's shared-memory opt-in, once per device
+    auto optin = [](PerDevice& once, const void* fn, int smem) {
+        return run_once(once, [&] {
+            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        });
+    };
+    cudaError_t e = cudaSuccess;
+    if (ws && vel) {
+        static PerDevice once;
+        const int smem = WMap<S, R, true>::bytes + 128;
+        if ((e = optin(once, (const void*)k_vel_ws<S, R>, smem)) != cudaSuccess) return e;
+        k_vel_ws<S, R><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+    } else if (ws) {
+        static PerDevice once;
+        const int smem = WMap<S, R, false>::bytes + 128;
+        if ((e = optin(once, (const void*)k_str_ws<S, R>, smem)) != cudaSuccess) return e;
+        k_str_ws<S, R><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+    } else if (vel) {
+        static PerDevice once;
         const int smem = Map<S, R, true>::bytes + 128;
-        static std::once_flag flag;
-        static cudaError_t status = cudaSuccess;
-        const cudaError_t e = run_once(flag, status, [&] {
-            return cudaFuncSetAttribute(k_vel<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        });
-        if (e != cudaSuccess) return e;
-        k_vel<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const VMaps*>(maps), g, p, zchunk);
+        if ((e = optin(once, (const void*)k_vel<S, R>, smem)) != cudaSuccess) return e;
+        k_vel<S, R><<<grid, NTH, smem, st>>>(vm, g, p, zchunk);
     } else {
+        static PerDevice once;
         const int smem = Map<S, R, false>::bytes + 128;
-        static std::once_flag flag;
-        static cudaError_t status = cudaSuccess;
-        const cudaError_t e = run_once(flag, status, [&] {
-            return cudaFuncSetAttribute(k_str<S, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        });
-        if (e != cudaSuccess) return e;
-        k_str<S, R><<<grid, NTH, smem, st>>>(*reinterpret_cast<const TMaps*>(maps), g, p, zchunk);
+        if ((e = optin(once, (const void*)k_str<S, R>, smem)) != cudaSuccess) return e;
+        k_str<S, R><<<grid, NTH, smem, st>>>(tm, g, p, zchunk);
     }
     return cudaGetLastError();
 }

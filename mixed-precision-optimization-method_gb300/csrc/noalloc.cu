@@ -15,7 +15,6 @@
 // that device current) and caches it; make that first call before any stream capture.  Every call
 // shares the array, so calls that overlap on the GPU (different streams, or different host threads)
 // race on it.  Each call rewrites the partials it reads, so nothing needs clearing between calls.
-#include <cfloat>
 #include <cstdio>
 #include <mutex>
 
@@ -34,7 +33,9 @@ constexpr int kMaxPartials = 65536;                                          // 
 constexpr long long kMaxCells = kCellsPerBlock * kMaxPartials;
 constexpr int kMaxDevices = 64;
 
-// One partial sum of squares per block; a negative entry marks a block that saw NaN/Inf/saturation.
+// One partial sum of squares per block over its finite, unsaturated cells; the sign bit marks a block that also
+// saw NaN/Inf/saturation (-0.0 when it saw nothing else), so the final sum keeps the finite cells of such blocks,
+// as behf_health does.
 static __device__ __align__(256) double g_norm_scratch[kMaxPartials];
 
 std::mutex g_scratch_mu;
@@ -66,7 +67,7 @@ __global__ void k_norm_part(const void* f, int nx, int ny, long long px, long lo
     if (threadIdx.x == 0) {
         double s = 0;
         for (int w = 0; w < kThreads / 32; w++) s += red[w];
-        part[blockIdx.x] = anybad ? -1.0 : s;
+        part[blockIdx.x] = anybad ? -s : s;  // s >= +0.0, so the sign bit carries only the flag
     }
 }
 
@@ -76,8 +77,8 @@ __global__ void k_norm_final(const double* part, int nb, double* norm_out, int* 
     int bad = 0;
     for (int b = threadIdx.x; b < nb; b += 32) {
         const double v = part[b];
-        if (v < 0) bad = 1;
-        else s += v;
+        if (signbit(v)) bad = 1;
+        s += fabs(v);
     }
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -149,7 +150,7 @@ extern "C" behf_status behf_field_norm_noalloc(const void* field, int precision,
         return BEHF_ERR_CUDA;
     }
     const int nb = (int)((N + kCellsPerBlock - 1) / kCellsPerBlock);
-    const double limit = precision == BEHF_FP16 ? 65504.0 : precision == BEHF_FP64 ? DBL_MAX : (double)FLT_MAX;
+    const double limit = behf::storage_max(precision);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (precision) {
         case BEHF_FP64: e = launch<double>(field, nx, ny, pitch, plane, N, limit, scratch, nb, norm_out, flag_out, st); break;

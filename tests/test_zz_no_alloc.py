@@ -29,7 +29,7 @@ def _noalloc_norm(values: np.ndarray, precision: str, pitch_pad: int, out, flag)
 
     import behf
     nz, ny, nx = values.shape
-    dt = {"f32": torch.float32, "f16": torch.float16}[precision]
+    dt = {"f64": torch.float64, "f32": torch.float32, "f16": torch.float16, "bf16": torch.bfloat16}[precision]
     pitch = nx + pitch_pad
     buf = torch.full((nz, ny, pitch), float("nan"), dtype=dt, device="cuda")  # padding must not be read
     buf[:, :, :nx] = torch.from_numpy(values).to(dt)
@@ -40,7 +40,7 @@ def _noalloc_norm(values: np.ndarray, precision: str, pitch_pad: int, out, flag)
     return int(flag.item()) == 0, float(out.item())
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16", "bf16"])
 def test_noalloc_matches_health_on_two_calls(behf_lib, precision):
     import torch
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -68,6 +68,22 @@ def test_noalloc_flags_nonfinite_then_recovers(behf_lib):
     ok_ref, ref = _health_norm(v, "f32")
     ok, got = _noalloc_norm(v, "f32", 3, out, flag)
     assert ok and ok_ref and got == pytest.approx(ref, rel=1e-12)
+
+
+@pytest.mark.parametrize("precision,top", [("f16", 65504.0), ("bf16", 3.3895313892515355e38)])
+def test_noalloc_flags_saturation_like_health(behf_lib, precision, top):
+    """A value at the largest finite value of the storage format is flagged by both entry points, and both
+    leave it out of the norm while keeping the other cells."""
+    import torch
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((10, 12, 14)).astype(np.float32)
+    v[3, 4, 5] = top
+    ok_ref, ref = _health_norm(v, precision)
+    ok, got = _noalloc_norm(v, precision, 2, out, flag)
+    assert not ok_ref and not ok
+    assert got == pytest.approx(ref, rel=1e-12) and 0 < got < 1e6
 
 
 def test_noalloc_rejects_fields_beyond_its_scratch(behf_lib):
