@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient (adjoint) measurement")
     ap.add_argument("--adjoint-n", type=int, default=256, help="grid of the gradient measurement")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--no-shots", action="store_true", help="skip the batched-shots measurement")
+    ap.add_argument("--shots-per-size", type=int, default=16)
+    ap.add_argument("--shots-steps", type=int, default=1500)
     ap.add_argument("--adjoint-only", action="store_true",
                     help="only the gradient measurement (one JSON object with the adjoint leg)")
     return ap.parse_args()
@@ -246,6 +249,53 @@ def adjoint_leg(args):
                            enumerate(("rho", "rhof", "mu", "M", "C", "HH", "H2U", "C1", "C2"))}}
 
 
+def shots_leg(args):
+    """Many independent shots on one GPU (48 shots: 16 each of 128^3, 192^3, 256^3, 1500 steps, FP16, radius 4,
+    20-cell CPML, layered + random medium from each shot's seed, 30 Hz pressure source at a seeded position, 128
+    receivers): batched on overlapping streams (behf_run_batch, graph-captured time loop) with the kernel variant
+    and z range the autotuner picked for each size, against the same shots run one after another with the default
+    kernels.  Medium generation is outside the timed regions."""
+    import torch
+
+    import behf
+    from behf import shots
+    sizes = [128, 192, 256]
+    per, nt, batch = args.shots_per_size, args.shots_steps, 4
+    cells_steps = sum(n ** 3 for n in sizes) * per * nt
+    t_seq, t_bat, tuned, launches = 0.0, 0.0, {}, 0
+    for n in sizes:
+        s = behf.solver_for(shots.shot_problem(n, 1000 * n, nt), precision=args.precision)
+        z, ms = s.autotune(3)
+        tuned[n] = {"variant": s.info()["tiled_variant"], "zchunk": z, "ms_per_step": ms}
+        s.close()
+        for i in range(per):
+            s = behf.solver_for(shots.shot_problem(n, 1000 * n + i, nt), precision=args.precision)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run(nt)
+            t_seq += time.perf_counter() - t0
+            s.close()
+        for g0 in range(0, per, batch):
+            group = [behf.solver_for(shots.shot_problem(n, 1000 * n + i, nt), precision=args.precision)
+                     for i in range(g0, min(per, g0 + batch))]
+            for s in group:
+                s.set_option(behf.OPT_TILED_VARIANT, {"classic": 1, "ws": 2, "tmem": 3}[tuned[n]["variant"]])
+                s.set_option(behf.OPT_ZCHUNK, tuned[n]["zchunk"])
+            l0 = sum(s.info()["launches"] for s in group)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            behf.run_batch(group, nt)
+            t_bat += time.perf_counter() - t0
+            launches += sum(s.info()["launches"] for s in group) - l0
+            for s in group:
+                s.close()
+    return {"workload": f"{per} shots each of {sizes} cells per axis, {nt} steps, {args.precision}, radius 4, "
+                        "20-cell CPML, layered + random medium per shot, pressure source 30 Hz, 128 receivers",
+            "sequential_s": t_seq, "batched_s": t_bat, "sequential_gpts": cells_steps / t_seq / 1e9,
+            "batched_gpts": cells_steps / t_bat / 1e9, "batched_over_sequential": t_seq / t_bat,
+            "batch": batch, "autotuned": tuned, "gpu_launches_batched": int(launches)}
+
+
 def behf_arm(args, world, rank, local):
     import torch
 
@@ -319,6 +369,10 @@ def behf_arm(args, world, rank, local):
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_leg(args)
 
+    shots_out = None
+    if rank == 0 and not args.no_shots:
+        shots_out = shots_leg(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, sec = cpu_rate(args.cpu_n, 6, 1)
@@ -340,7 +394,8 @@ def behf_arm(args, world, rank, local):
                "kernel_ms": kt, "kernel_family": info["kernel"], "scales": info["scales"], "health_ok": ok,
                "fp32": fp32, "fp16_over_fp32": (value / world / fp32["auto"]) if fp32 else None,
                "fp16_over_plain_fp32": (value / world / fp32["plain"]) if fp32 else None,
-               "clocks": clocks, "cpu_baseline": cpu, "device_bytes": info["device_bytes"], "adjoint": adjoint}
+               "clocks": clocks, "cpu_baseline": cpu, "device_bytes": info["device_bytes"], "adjoint": adjoint,
+               "shots": shots_out}
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

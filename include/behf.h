@@ -80,6 +80,8 @@ typedef struct {
     int kernel;              /* kernel family in use (behf_kernel) */
     int radius, precision;
     int64_t launches;        /* kernels enqueued by this context so far (graph launches count their nodes) */
+    int tiled_variant;       /* tiled kernels in use: 1 classic, 2 warp-specialised, 3 warp-specialised + TMEM z */
+    int zchunk;              /* z planes per CTA requested for the tiled kernels (0 = automatic) */
 } behf_info;
 
 /* Kernel family: PLAIN = one thread per cell with cached neighbour loads; TILED = the z-marching
@@ -108,9 +110,14 @@ enum {
     BEHF_OPT_CHECKPOINT_OUTER = 9, /* gradient: outer checkpoint spacing of the two-level scheme, rounded up to a
                                     multiple of BEHF_OPT_CHECKPOINT (0 = automatic: one level when it fits the
                                     device memory, else two levels with the inner spacing halved until they fit) */
-    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic, 1 = classic (own-cell data by direct loads of the
+    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic (3 for FP16 / BF16, 2 for FP32), 1 = classic (own-cell data by direct loads of the
                                     compute threads), 2 = warp-specialised (a producer warp brings every input,
-                                    own-cell data included, through TMA) */
+                                    own-cell data included, through TMA), 3 = warp-specialised with the z derivatives
+                                    accumulated plane by plane in tensor memory (TMEM) */
+    BEHF_OPT_GRAD_COMPENSATION = 11, /* gradient with an FP32 adjoint (16/32-bit kinds): the coefficient-gradient
+                                    accumulators sum each checkpoint segment in FP32, then fold it into running
+                                    totals: 1 = Neumaier-compensated FP32 totals (default), 0 = no fold (plain FP32
+                                    accumulation over all steps), 2 = FP64 totals (reference for the error) */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current
@@ -256,9 +263,10 @@ behf_status behf_physical_gradient(long long ncell, const float* const moduli[BE
                                    const double* const grad_moduli[BEHF_NMOD], double eta,
                                    double* const grad_phys[BEHF_NPHYS]);
 
-/* Autotuner (no counterpart in the reference): times trial_steps steps for each z-chunk length of the tiled
- * kernels (BEHF_OPT_ZCHUNK candidates 0, 16, 32, ... up to the grid), keeps the fastest, and resets the
- * wavefields (behf_reset).  Writes the chosen value and its milliseconds per step. */
+/* Autotuner (no counterpart in the reference, which fixes its 16 x 8 block, kernel.cu:17-19): times trial_steps
+ * steps for each tiled-kernel variant (BEHF_OPT_TILED_VARIANT 1..3) and each z-chunk length (BEHF_OPT_ZCHUNK
+ * candidates 0, 16, 32, ... up to the grid), keeps the fastest pair, and resets the wavefields (behf_reset).
+ * Writes the chosen z-chunk and its milliseconds per step; the chosen variant is in behf_info.tiled_variant. */
 behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, double* ms_per_step_out);
 
 /* Batched shots on one GPU (no counterpart in the reference): advances n independent contexts by nsteps each,

@@ -14,7 +14,11 @@ Named workloads (sizes, steps and media of the benchmark and parity cases):
     small64       64^3, h = 5 m, dt = 0.4 ms, 500 steps, 10-cell CPML, homogeneous sandstone,
                   explosive source at the centre, 30 Hz Ricker, 32 receivers on a line (vz and p)
     layered256    256^3, 2000 steps, 20-cell CPML, sandstone over a stiffer layer at z = 640 m,
-                  25 Hz explosive source, 16 x 16 surface receivers (vz and p)
+                  25 Hz explosive (pressure) source, 16 x 16 surface receivers (vz and p).  The source is the
+                  isotropic-stress "explosive (pressure)" source of small64 and of the reference (kernel.cu:130-142),
+                  not an injection into the pore pressure: in this medium a pore-pressure injection radiates a fast
+                  wave 1e-4 to 1e-5 of the near-source pressure, which FP32 storage already resolves only to
+                  1.7e-3 (oracle, 64^3) and FP16 storage not at all
     random1024    1024^3, 3000 steps, 20-cell CPML, sandstone with 5 % Gaussian-correlated (50 m)
                   perturbations of K_dry, mu, phi and log-normal kappa (sigma 0.5), vertical force
                   source, 20 Hz, 512 x 512 surface receivers (vz and p)

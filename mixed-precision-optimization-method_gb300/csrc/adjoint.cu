@@ -1210,6 +1210,36 @@ cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Neumaier summation: the total and the compensation of each accumulator (FP32), or an FP64 total.  One thread per
+// cell index, every accumulator in turn; g is zeroed for the next segment.
+__global__ void k_adj_fold(AdjFold f, long long n, int final) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        for (int q = 0; q < kNCoef; q++) {
+            const float y = f.g[q][i];
+            if (f.mode == 2) {
+                const double t = f.tot64[q][i] + (double)y;
+                if (final) f.g[q][i] = (float)t;
+                else {
+                    f.tot64[q][i] = t;
+                    f.g[q][i] = 0.f;
+                }
+            } else {
+                const float t = f.tot[q][i], s = t + y;
+                const float c = f.comp[q][i] + (fabsf(t) >= fabsf(y) ? (t - s) + y : (y - s) + t);
+                if (final) f.g[q][i] = s + c;
+                else {
+                    f.tot[q][i] = s;
+                    f.comp[q][i] = c;
+                    f.g[q][i] = 0.f;
+                }
+            }
+        }
+}
+cudaError_t adj_fold(const AdjFold& f, long long n, int final, cudaStream_t st) {
+    k_adj_fold<<<device_sms() * 8, 256, 0, st>>>(f, n, final);
+    return cudaGetLastError();
+}
+
 #define BEHF_ADJ_INST(S)                                                                                         \
     template cudaError_t adj_build_maps<S>(const Geom&, const AdjPtrs&, AdjMaps*);                             \
     template bool adj_snap_staged<S>();                                                                        \

@@ -100,4 +100,18 @@ struct GradModArgs {
 };
 template <class A> cudaError_t adj_grad_moduli(const GradModArgs& a, cudaStream_t st);
 
+// Compensated summation of the FP32 coefficient-gradient accumulators.  The backward steps of one checkpoint
+// segment add into g[] (FP32) as before; at the segment's end adj_fold moves each g[q][i] into a running total
+// and zeroes it: mode 1 Neumaier-compensated FP32 (tot += g with the lost low-order part kept in comp), mode 2
+// an FP64 total (the reference for measuring the accumulation error).  final = 1 writes tot + comp (mode 1) or the
+// rounded FP64 total (mode 2) back into g[] for the moduli transpose.
+struct AdjFold {
+    float* g[kNCoef];
+    float* tot[kNCoef];
+    float* comp[kNCoef];
+    double* tot64[kNCoef];
+    int mode;
+};
+cudaError_t adj_fold(const AdjFold& f, long long n, int final, cudaStream_t st);
+
 }  // namespace behf

@@ -22,6 +22,12 @@ using namespace behf;
 namespace {
 thread_local std::string g_err;
 
+// Tiled-kernel variant chosen by BEHF_OPT_TILED_VARIANT = 0 (Geom::ws): the warp-specialised kernels with the z
+// derivatives in tensor memory for the 16-bit kinds, the warp-specialised kernels for FP32 (1024^3 on one GB300:
+// FP16 30.5 / 33.7 / 35.2, BF16 28.7 / 32.1 / 34.0, FP32 20.8 / 21.7 / 21.2 Gpt/s for classic / warp-specialised /
+// tensor-memory z).
+int auto_variant(int precision) { return precision == BEHF_FP16 || precision == BEHF_BF16 ? 2 : 1; }
+
 behf_status fail(behf_status code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -131,6 +137,7 @@ struct behf_ctx {
     int ck_stride = 0;
     int ck_outer = 0;  // gradient: outer checkpoint spacing of the two-level scheme (0 automatic)
     int snap_cache_mib = -1;  // gradient: device memory for snapshots kept from the forward pass (-1 automatic)
+    int grad_comp = 1;    // gradient: FP32 accumulators folded per segment (0 plain, 1 Neumaier, 2 FP64 total)
     int coef_dither = 0;  // BEHF_OPT_COEF_ROUNDING
 
     ~behf_ctx() {
@@ -502,7 +509,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.plane = g.px * gr->ny;
     g.bug = 0;
     g.zchunk_req = 0;
-    g.ws = 0;
+    g.ws = auto_variant(precision);
     g.sr = 0;
     g.step = nullptr;
     g.step_off = 0;
@@ -921,9 +928,13 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0) return fail(BEHF_ERR_INVALID, "negative z chunk");
             c->g.zchunk_req = value;
             break;
+        case BEHF_OPT_GRAD_COMPENSATION:
+            if (value < 0 || value > 2) return fail(BEHF_ERR_INVALID, "gradient compensation must be 0, 1 or 2");
+            c->grad_comp = value;
+            break;
         case BEHF_OPT_TILED_VARIANT:
-            if (value < 0 || value > 2) return fail(BEHF_ERR_INVALID, "tiled variant must be 0, 1 or 2");
-            c->g.ws = value == 2 ? 1 : 0;
+            if (value < 0 || value > 3) return fail(BEHF_ERR_INVALID, "tiled variant must be 0, 1, 2 or 3");
+            c->g.ws = value == 0 ? auto_variant(c->prec) : value - 1;
             break;
         default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
     }
@@ -946,6 +957,8 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
     out->radius = c->g.R;
     out->precision = c->prec;
     out->launches = c->launches;
+    out->tiled_variant = c->g.ws + 1;
+    out->zchunk = c->g.zchunk_req;
     return BEHF_OK;
 }
 
@@ -1146,6 +1159,25 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
     a.grad = 1;
     a.derived = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? 1 : 0;
+    // compensated summation of the FP32 accumulators: segment sums folded into running totals
+    AdjFold fold{};
+    const bool folding = sizeof(A) == 4 && c->grad_comp > 0;
+    if (folding) {
+        fold.mode = c->grad_comp;
+        for (int q = 0; q < kNCoef && !st; q++) {
+            fold.g[q] = reinterpret_cast<float*>(a.g[q]);
+            if (fold.mode == 2) {
+                st = buf.get((void**)&fold.tot64[q], nf * 8);
+                if (!st) CK(cudaMemsetAsync(fold.tot64[q], 0, nf * 8, c->stream));
+            } else {
+                st = buf.get((void**)&fold.tot[q], nf * 4);
+                if (!st) st = buf.get((void**)&fold.comp[q], nf * 4);
+                if (!st) CK(cudaMemsetAsync(fold.tot[q], 0, nf * 4, c->stream));
+                if (!st) CK(cudaMemsetAsync(fold.comp[q], 0, nf * 4, c->stream));
+            }
+        }
+        if (st) return st;
+    }
     AdjMaps* maps = static_cast<AdjMaps*>(std::aligned_alloc(alignof(AdjMaps), sizeof(AdjMaps)));
     if (!maps) return fail(BEHF_ERR_ALLOC, "host allocation of the adjoint tensor maps");
     std::unique_ptr<AdjMaps, void (*)(void*)> maps_owner(maps, std::free);
@@ -1336,7 +1368,15 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                                      c->stream));
                 c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
             }
+            if (folding) {
+                CK(adj_fold(fold, (long long)nf, 0, c->stream));
+                c->launches++;
+            }
         }
+    }
+    if (folding) {
+        CK(adj_fold(fold, (long long)nf, 1, c->stream));
+        c->launches++;
     }
     CK(cudaMemcpyAsync(c->d_it, &nt, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     st = behf_sync(c);
@@ -1459,18 +1499,24 @@ behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double*
     if (!c->medium_set) return fail(BEHF_ERR_STATE, "behf_set_medium must come before behf_autotune");
     if (trial_steps < 1) return fail(BEHF_ERR_INVALID, "trial_steps must be positive");
     const int planes = c->grid.nz - 2 * c->g.R;
-    std::vector<int> cand = {0};
-    for (int z = 16; z < planes; z *= 2) cand.push_back(z);
-    cand.push_back(planes);
+    std::vector<int> zc = {0};
+    for (int z = 16; z < planes; z *= 2) zc.push_back(z);
+    zc.push_back(planes);
+    // (variant, z chunk) pairs: the variants only where the tiled kernels run
+    std::vector<std::pair<int, int>> cand;
+    const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok;
+    for (int v = tiled ? 0 : c->g.ws; v <= (tiled ? 2 : c->g.ws); v++)
+        for (int z : zc) cand.push_back({v, z});
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     double best = 1e300;
-    int best_z = 0;
+    int best_z = 0, best_v = c->g.ws;
     behf_status st = BEHF_OK;
     const int nrec = c->nrec;
     c->nrec = 0;  // trial steps record nothing
-    for (int z : cand) {
+    for (auto [v, z] : cand) {
+        c->g.ws = v;
         c->g.zchunk_req = z;
         c->invalidate_graph();
         if ((st = zero_state(c))) break;
@@ -1484,11 +1530,13 @@ behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double*
         if (ms / trial_steps < best) {
             best = ms / trial_steps;
             best_z = z;
+            best_v = v;
         }
     }
     c->nrec = nrec;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    c->g.ws = best_v;
     c->g.zchunk_req = best_z;
     c->invalidate_graph();
     if (st) return st;

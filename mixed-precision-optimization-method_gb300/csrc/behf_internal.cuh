@@ -115,7 +115,8 @@ struct Geom {
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out
     int zchunk_req;        // tiled kernels: z planes per CTA (0 = automatic)
-    int ws;                // tiled kernels: 1 = warp-specialised variant (every read through TMA), 0 = classic
+    int ws;                // tiled kernels: 0 = classic, 1 = warp-specialised (every read through TMA), 2 = the same
+                           // with the z derivatives accumulated in tensor memory
     int sr;                // 16-bit kinds, tiled kernels: stochastic rounding of the stored fields
     const int* step;       // device step counter (seeds the stochastic rounding)
     int step_off;          // step offset of this launch within a graph chunk

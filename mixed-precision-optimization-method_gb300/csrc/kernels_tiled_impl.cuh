@@ -598,6 +598,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
 }  // namespace behf
 
 #include "kernels_tiled_ws.cuh"
+#include "kernels_tiled_zq.cuh"
 
 namespace behf {
 namespace tiled {
@@ -656,7 +657,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // that, a chunk count that fills the last wave of resident CTAs (MINB per SM) with at least four waves where
     // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
     // for two waves of 36-plane chunks)
-    const bool ws = g.ws != 0;
+    const bool ws = g.ws != 0, zq = g.ws == 2;
     const int minb = ws ? WDepth<S>::MINB : vel ? Depth<S>::MINB : Depth<S>::MINB_T;
     const int slots = minb * device_sms();
     int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, BEHF_TILED_MINW);
@@ -671,7 +672,17 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
         });
     };
     cudaError_t e = cudaSuccess;
-    if (ws && vel) {
+    if (zq && vel) {
+        static PerDevice once;
+        const int smem = ZMap<S, R, true>::bytes + 128;
+        if ((e = optin(once, (const void*)k_vel_zq<S, R>, smem)) != cudaSuccess) return e;
+        k_vel_zq<S, R><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+    } else if (zq) {
+        static PerDevice once;
+        const int smem = ZMap<S, R, false>::bytes + 128;
+        if ((e = optin(once, (const void*)k_str_zq<S, R>, smem)) != cudaSuccess) return e;
+        k_str_zq<S, R><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+    } else if (ws && vel) {
         static PerDevice once;
         const int smem = WMap<S, R, true>::bytes + 128;
         if ((e = optin(once, (const void*)k_vel_ws<S, R>, smem)) != cudaSuccess) return e;

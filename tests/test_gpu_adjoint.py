@@ -176,3 +176,88 @@ def test_torch_autograd_wrapper(behf_lib):
     assert abs(loss.item() - J) <= 1e-10 * J
     assert rel(mod.grad.double().cpu().numpy(), gm.astype(np.float32).astype(np.float64)) < 1e-6
     assert rel(w.grad.double().numpy(), gw.astype(np.float32).astype(np.float64)) < 1e-6
+
+
+def _inversion_case(n=48, nt=300, true_model=False, cpml=8):
+    """The gradient workload (two-layer medium, 100 m anomaly of -10 % K_dry and x10 kappa in the true model,
+    pressure source, surface receivers of vz and p) on n^3 cells of 5 m, with host moduli."""
+    p = P.inversion256(n=n, nt=nt, true_model=true_model, cpml=cpml, nrec_side=8)
+    sp = p.extra["spec"]
+    mod = P.spec_medium((n, n, n), sp["layers"], sp["interfaces"], sp["seed"], sp["corr_cells"], sp["pct"],
+                        sp["log_kappa_sigma"], sp["anomaly"])
+    return dataclasses.replace(p, mod=mod)
+
+
+def test_gradient_48_matches_cpu_fp64_adjoint(behf_lib, oracle):
+    """The 48^3 sub-case of the gradient workload: the GPU gradient (FP64 storage) against the FP64 CPU discrete
+    adjoint of the oracle, in the moduli and in the physical parameters."""
+    p = _inversion_case()
+    dobs = oracle.run(_inversion_case(true_model=True), "f64")[0]
+    s = behf.solver_for(p, precision="f64", gradient=True)
+    J, gw, gm = s.misfit_gradient(p.nt, dobs)
+    seis = s.seismograms()
+    s.close()
+    assert J > 0
+    ref = oracle.adjoint(p, seis - dobs)
+    assert rel(gw, ref["grad_wavelet"]) < 1e-9
+    for q in range(9):
+        assert rel(gm[q], ref["grad_mod"][q]) < 1e-8, q
+    gp, gp_ref = behf.physical_gradient(p.mod, gm), behf.physical_gradient(p.mod, ref["grad_mod"])
+    for q in range(7):
+        assert np.abs(gp_ref[q]).max() > 0, behf.PHYSICAL[q]
+        assert rel(gp[q], gp_ref[q]) < 1e-8, behf.PHYSICAL[q]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_physical_gradient_central_differences(behf_lib, seed):
+    """Central differences of the FP64 misfit along a random seeded direction that perturbs all seven physical
+    parameters of every cell of the inverted region at once (relative steps +-1e-3)."""
+    p = _inversion_case(n=26, nt=120, cpml=4)
+    n = p.nx
+    dobs = _forward_f64(_inversion_case(n=26, nt=120, true_model=True, cpml=4))
+    s = behf.solver_for(p, precision="f64", gradient=True)
+    J, _, gm = s.misfit_gradient(p.nt, dobs)
+    s.close()
+    gp = behf.physical_gradient(p.mod, gm)
+    phys, ratio = P.physical_from_moduli(p.mod)
+    rng = np.random.default_rng(100 + seed)
+    d = rng.standard_normal(phys.shape)
+    m = p.cpml_width + p.radius + 2  # the inverted region (cells whose coefficient cells lie outside the slabs)
+    mask = np.zeros((n, n, n), bool)
+    mask[m:n - m, m:n - m, m:n - m] = True
+    d *= mask
+    eps = 1e-3
+    php, phm = phys * (1 + eps * d), phys * (1 - eps * d)
+    jp = 0.5 * ((_forward_f64(dataclasses.replace(p, mod=P.moduli_from_physical(php, ratio))) - dobs) ** 2).sum()
+    jm = 0.5 * ((_forward_f64(dataclasses.replace(p, mod=P.moduli_from_physical(phm, ratio))) - dobs) ** 2).sum()
+    fd = jp - jm
+    pred = float((gp * (php - phm)).sum())
+    assert abs(fd - pred) <= 1e-3 * abs(fd), (fd, pred)
+
+
+def _forward_f64(p):
+    s = behf.solver_for(p, precision="f64")
+    s.run(p.nt)
+    d = s.seismograms()
+    s.close()
+    return d
+
+
+def test_gradient_compensated_accumulation(behf_lib, oracle):
+    """FP32 adjoint over 400 steps: the Neumaier-folded accumulators (the default) are at least as close to the
+    FP64-folded ones as plain FP32 accumulation over all steps, and all three within 1e-4 of the FP64 oracle."""
+    p = small(n=22, nt=400, R=2, L=4, kind="explosive")
+    adj = np.random.default_rng(9).standard_normal((len(p.rec_comp), p.nt))
+    ref = oracle.adjoint(p, adj)
+    out = {}
+    for mode in (0, 1, 2):
+        s = behf.solver_for(p, precision="f32", gradient=True, checkpoint=20)
+        s.set_option(behf.OPT_GRAD_COMPENSATION, mode)
+        _, gm = s.gradient(p.nt, adj)
+        s.close()
+        out[mode] = gm
+    for q in range(9):
+        e_plain, e_comp = rel(out[0][q], out[2][q]), rel(out[1][q], out[2][q])
+        assert e_comp <= e_plain + 1e-9, (q, e_plain, e_comp)
+        for mode in (0, 1, 2):
+            assert rel(out[mode][q], ref["grad_mod"][q]) < 1e-4, (q, mode)

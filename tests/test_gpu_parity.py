@@ -107,11 +107,14 @@ def test_final_wavefields_match(behf_lib, oracle):
     s.close()
 
 
-def test_reference_layout_problem(behf_lib, oracle):
-    """Radius 1, the reference's scales and the vz/VW3y compatibility, heterogeneous medium."""
+@pytest.mark.parametrize("golden", ["ref_rock", "ref_borehole"])
+def test_reference_layout_problem(behf_lib, oracle, golden):
+    """Radius 1, the reference's scales and the vz/VW3y compatibility: a heterogeneous rock, and the reference's
+    own fluid-filled borehole medium (outputfunc.cpp:153-222, h = 1 cm, dt = 1 us, 10 kHz), against the FP64
+    oracle and against the reference kernels' own FP16 run of the same problem (the golden fixture)."""
     from behf import problems
     from conftest import load_golden
-    g = load_golden("ref_rock")
+    g = load_golden(golden)
     nz, ny, nx = (int(v) for v in g["shape"])
     rl = g["rec_lin"].astype(np.int64)
     ijk = np.stack([rl % nx, (rl // nx) % ny, rl // (nx * ny)], 1).astype(np.int32)
