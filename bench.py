@@ -240,7 +240,8 @@ def adjoint_leg(args):
     launches = s.info()["launches"] - l0
     s.close()
     fwd, grad = t1 - t0, t3 - t2
-    return {"workload": f"inversion{n}: {n}^3 two-layer medium, anomaly-free start model, pressure source 25 Hz, "
+    return {"workload": f"inversion{n}: {n}^3 two-layer medium, anomaly-free start model, explosive (pressure) "
+                        f"source 25 Hz, "
                         f"{len(prob.rec_comp)} traces (vz, p), L2 misfit",
             "steps": nt, "storage": args.precision, "adjoint_arithmetic": "f64" if args.precision == "f64" else "f32",
             "checkpoint_every": int(round(nt ** 0.5)), "forward_s": fwd, "gradient_s_per_shot": grad,
@@ -251,8 +252,8 @@ def adjoint_leg(args):
 
 def shots_leg(args):
     """Many independent shots on one GPU (48 shots: 16 each of 128^3, 192^3, 256^3, 1500 steps, FP16, radius 4,
-    20-cell CPML, layered + random medium from each shot's seed, 30 Hz pressure source at a seeded position, 128
-    receivers): batched on overlapping streams (behf_run_batch, graph-captured time loop) with the kernel variant
+    20-cell CPML, layered + random medium from each shot's seed, 30 Hz explosive (pressure) source at a seeded
+    position, 128 receivers): batched on overlapping streams (behf_run_batch, graph-captured time loop) with the kernel variant
     and z range the autotuner picked for each size, against the same shots run one after another with the default
     kernels.  Medium generation is outside the timed regions."""
     import torch
@@ -290,7 +291,8 @@ def shots_leg(args):
             for s in group:
                 s.close()
     return {"workload": f"{per} shots each of {sizes} cells per axis, {nt} steps, {args.precision}, radius 4, "
-                        "20-cell CPML, layered + random medium per shot, pressure source 30 Hz, 128 receivers",
+                        "20-cell CPML, layered + random medium per shot, explosive (pressure) source 30 Hz, "
+                        "128 receivers",
             "sequential_s": t_seq, "batched_s": t_bat, "sequential_gpts": cells_steps / t_seq / 1e9,
             "batched_gpts": cells_steps / t_bat / 1e9, "batched_over_sequential": t_seq / t_bat,
             "batch": batch, "autotuned": tuned, "gpu_launches_batched": int(launches)}

@@ -23,7 +23,7 @@ Named workloads (sizes, steps and media of the benchmark and parity cases):
                   perturbations of K_dry, mu, phi and log-normal kappa (sigma 0.5), vertical force
                   source, 20 Hz, 512 x 512 surface receivers (vz and p)
     inversion256  the gradient workload: layered256's medium (+ a 100 m Gaussian anomaly for the true model),
-                  16 pressure-source shots at 25 Hz, 2000 steps, 16 x 16 surface receivers (vz and p)
+                  16 explosive (pressure) source shots at 25 Hz, 2000 steps, 16 x 16 surface receivers (vz and p)
     borehole      the reference's own problem: 240 x 240 x 360 cells of 1 cm (180^2 x 300 + 30-cell
                   CPML), fluid borehole in a porous formation, 10 kHz, 3500 steps of 1 us, radius 1,
                   txx recorded on the vertical line through the source (main.cpp:20-23, 84-99)
@@ -298,8 +298,9 @@ def layered256(n=256, nt=2000, radius=4, cpml=20, nrec_side=16) -> Problem:
 def inversion256(n=256, nt=2000, shot=0, true_model=True, radius=4, cpml=20, nrec_side=16) -> Problem:
     """The gradient workload: the two-layer 256^3 medium of layered256 (interface at z = 640 m), for the true
     model with a Gaussian anomaly of 100 m radius (K_dry -10 %, kappa x10) above the interface; 25 Hz
-    pressure source of shot `shot` (one of 16 on a 4 x 4 grid at depth L + 6), 16 x 16 surface receivers
-    recording vz and p.  The medium is left to the device generator (extra["spec"])."""
+    explosive (pressure) source of shot `shot` (one of 16 on a 4 x 4 grid at depth L + 6; the source kind of
+    layered256, for the reason given there), 16 x 16 surface receivers recording vz and p.  The medium is left to
+    the device generator (extra["spec"])."""
     h, dt, f0 = 5.0, 4e-4, 25.0
     zi = n // 2
     anomaly = dict(center=(n / 2, n / 2, 0.78 * zi), radius=100.0 / h, dkdry=-0.10, kappa_factor=10.0)
@@ -311,7 +312,7 @@ def inversion256(n=256, nt=2000, shot=0, true_model=True, radius=4, cpml=20, nre
     grid = np.linspace(cpml + 10, n - cpml - 11, 4).round().astype(int)
     src = (int(grid[shot % 4]), int(grid[(shot // 4) % 4]), cpml + 6)
     return Problem(n, n, n, h, dt, radius, np.zeros((9, 1, 1, 1), np.float32), ricker(nt, dt, f0), src, ijk, comp,
-                   src_kind="pressure", cpml_width=cpml, cpml_v0=p_velocity(STIFF), f0=f0,
+                   src_kind="explosive", cpml_width=cpml, cpml_v0=p_velocity(STIFF), f0=f0,
                    name=f"inversion{n}", extra={"spec": spec, "shot": shot})
 
 

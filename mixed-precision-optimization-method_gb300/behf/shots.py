@@ -3,7 +3,7 @@
     python -m behf.shots [--per-size 16] [--sizes 128,192,256] [--steps 1500] [--batch 4] [--precision f16]
 
 The shot workload: per grid size, `per-size` shots, each its own medium (two layers with the interface at
-mid-depth, 5 % Gaussian-correlated perturbations from the shot's seed), a 30 Hz pressure source at a
+mid-depth, 5 % Gaussian-correlated perturbations from the shot's seed), a 30 Hz explosive (pressure) source at a
 seeded random position 6 cells below the top CPML, 128 receivers (vz, p) on a surface line, 20-cell CPML,
 radius 4.  Set-up (medium generation, coefficients) is outside the timed region; the time is the run only.
 Prints one JSON object: Gpt-updates/s sequential, batched, and the autotuned z-chunk of each size.
@@ -29,7 +29,7 @@ def shot_problem(n: int, seed: int, nt: int = 1500, cpml: int = 20) -> P.Problem
     xs = np.linspace(cpml + 2, n - cpml - 3, 64).round().astype(int)
     ijk, comp = P.line_receivers(xs, n // 2, cpml + 2, [2, 12])
     return P.Problem(n, n, n, h, dt, 4, np.zeros((9, 1, 1, 1), np.float32), P.ricker(nt, dt, f0),
-                     (sx, sy, cpml + 6), ijk, comp, src_kind="pressure", cpml_width=cpml,
+                     (sx, sy, cpml + 6), ijk, comp, src_kind="explosive", cpml_width=cpml,
                      cpml_v0=P.p_velocity(P.STIFF), f0=f0, name=f"shot{n}_{seed}", extra={"spec": spec})
 
 
@@ -45,7 +45,8 @@ def main(argv=None):
     args = ap.parse_args(argv)
     sizes = [int(v) for v in args.sizes.split(",")]
     out = {"workload": f"{args.per_size} shots per size {sizes}, {args.steps} steps, radius 4, 20-cell CPML, "
-                       f"pressure source 30 Hz, 128 receivers", "precision": args.precision, "batch": args.batch}
+                       f"explosive (pressure) source 30 Hz, 128 receivers", "precision": args.precision,
+           "batch": args.batch}
     cells_steps = sum(n ** 3 for n in sizes) * args.per_size * args.steps
     # sequential
     t_seq, tune = 0.0, {}

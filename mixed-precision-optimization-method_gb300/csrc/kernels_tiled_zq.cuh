@@ -233,6 +233,9 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     const int oe = ty * TXC + xl;
     const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x2545f491u) : 0u;
     const uint32_t ta = tbase + ((uint32_t)(32 * (ty & 3)) << 16) + (uint32_t)(ty >> 2) * 64u;
+    // x and y of a thread are fixed: whether its cells lie in an x or y slab is decided once, z per plane
+    const bool xy_slab = g.W > 0 && live && ((a0 && slab_index(x, g.nx, g.L) >= 0) ||
+                                             (a1 && slab_index(x + 1, g.nx, g.L) >= 0) || slab_index(y, g.ny, g.L) >= 0);
     // z fields: tzz (fwd), txz (bwd), tyz (bwd), p (fwd); box(f) gives field f's plane of cell pairs
     auto zsteps = [&](auto box, float2& d0, float2& d1, float2& d2, float2& d3) {
         auto val = [&](int f) { return PS::f2(*reinterpret_cast<const P*>(box(f) + oe * sizeof(S))); };
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         }
         if (live) {
             const long long go = (long long)k * g.plane + col;
-            if (g.W > 0) {
+            if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
                 const bool hf[4] = {true, true, false, false};
                 pml_pair<0>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
             }
@@ -413,6 +416,8 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     const int oe = ty * TXC + xl;
     const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x6a09e667u) : 0u;
     const uint32_t ta = tbase + ((uint32_t)(32 * (ty & 3)) << 16) + (uint32_t)(ty >> 2) * 64u;
+    const bool xy_slab = g.W > 0 && live && ((a0 && slab_index(x, g.nx, g.L) >= 0) ||
+                                             (a1 && slab_index(x + 1, g.nx, g.L) >= 0) || slab_index(y, g.ny, g.L) >= 0);
     // z fields: vx (fwd), vy (fwd), vz (bwd), qz (bwd); box(f) gives field f's plane of cell pairs
     auto zsteps = [&](auto box, float2& d0, float2& d1, float2& d2, float2& d3) {
         auto val = [&](int f) { return PS::f2(*reinterpret_cast<const P*>(box(f) + oe * sizeof(S))); };
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         }
         if (live) {
             const long long go = (long long)k * g.plane + col;
-            if (g.W > 0) {
+            if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
                 const bool hf[4] = {false, false, true, true};
                 pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
             }
