@@ -23,7 +23,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE_TREE = Path(os.environ.get("BEHF_REFERENCE_TREE", "/root/reference"))
+# The read-only reference checkout: BEHF_REFERENCE_TREE, else a directory named "reference" beside this repository
+# (where the build container mounts it; the GPU machines have none and use the committed fixtures).
+REFERENCE_TREE = Path(os.environ.get("BEHF_REFERENCE_TREE") or HERE.parent.parent / "reference")
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 
