@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="behf", choices=["behf", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="grid cells per axis")
+    ap.add_argument("--cpml", type=int, default=20, help="CPML cells per face (20 at 1024^3; 7 at 384^3 gives the "
+                    "same slab fraction of the grid)")
     ap.add_argument("--precision", default="f16", choices=["f16", "bf16", "f32", "f64"])
     ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "tiled"])
     ap.add_argument("--no-e2e", action="store_true")
@@ -170,7 +172,7 @@ def reference_arm(args, world, rank):
 
 
 def config_dict(args):
-    return {"workload": f"random{args.n}: {args.n}^3 cells, h=5 m, dt=0.4 ms, radius 4, 20-cell CPML, "
+    return {"workload": f"random{args.n}: {args.n}^3 cells, h=5 m, dt=0.4 ms, radius 4, {args.cpml}-cell CPML, "
                         "5% Gaussian-correlated sandstone, force source 20 Hz, 512x512 receivers (vz,p)",
             "grid": [args.n] * 3, "storage": args.precision, "kernel": args.kernel,
             "parallelism": f"replicas x{args.gpus}", "l2": "no flush: working set ~96 GB >> 129 MB L2"}
@@ -311,7 +313,7 @@ def behf_arm(args, world, rank, local):
     ktime = 3
     e2e_steps = 0 if args.no_e2e else max(args.steps // 2, 3)
     total = args.warmup + args.steps + ktime + e2e_steps
-    prob = problems.random1024(n=n, nt=total, medium=False)
+    prob = problems.random1024(n=n, nt=total, medium=False, cpml=args.cpml)
     cells = prob.cells
     s = make_solver(prob, args.precision, args.kernel, total)
     s.run(args.warmup)
@@ -393,7 +395,8 @@ def behf_arm(args, world, rank, local):
                "step_roofline": {"bytes_per_cell_fused": ab["step_fused"], "bytes_per_cell_unfused": ab["step_unfused"],
                                  "achieved": value / world * ab["step_fused"], "frac": value / world * ab["step_fused"] / peak,
                                  "roofline_gpts": peak / ab["step_fused"]},
-               "kernel_ms": kt, "kernel_family": info["kernel"], "scales": info["scales"], "health_ok": ok,
+               "kernel_ms": kt, "kernel_family": info["kernel"], "kernel_variant": info["tiled_variant"],
+               "scales": info["scales"], "health_ok": ok,
                "fp32": fp32, "fp16_over_fp32": (value / world / fp32["auto"]) if fp32 else None,
                "fp16_over_plain_fp32": (value / world / fp32["plain"]) if fp32 else None,
                "clocks": clocks, "cpu_baseline": cpu, "device_bytes": info["device_bytes"], "adjoint": adjoint,

@@ -675,13 +675,25 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     if (zq && vel) {
         static PerDevice once;
         const int smem = ZMap<S, R, true>::bytes + 128;
-        if ((e = optin(once, (const void*)k_vel_zq<S, R>, smem)) != cudaSuccess) return e;
-        k_vel_zq<S, R><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+        if (g.sr && sizeof(S) == 2) {
+            static PerDevice once_sr;
+            if ((e = optin(once_sr, (const void*)k_vel_zq<S, R, true>, smem)) != cudaSuccess) return e;
+            k_vel_zq<S, R, true><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+        } else {
+            if ((e = optin(once, (const void*)k_vel_zq<S, R, false>, smem)) != cudaSuccess) return e;
+            k_vel_zq<S, R, false><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+        }
     } else if (zq) {
         static PerDevice once;
         const int smem = ZMap<S, R, false>::bytes + 128;
-        if ((e = optin(once, (const void*)k_str_zq<S, R>, smem)) != cudaSuccess) return e;
-        k_str_zq<S, R><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+        if (g.sr && sizeof(S) == 2) {
+            static PerDevice once_sr;
+            if ((e = optin(once_sr, (const void*)k_str_zq<S, R, true>, smem)) != cudaSuccess) return e;
+            k_str_zq<S, R, true><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+        } else {
+            if ((e = optin(once, (const void*)k_str_zq<S, R, false>, smem)) != cudaSuccess) return e;
+            k_str_zq<S, R, false><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+        }
     } else if (ws && vel) {
         static PerDevice once;
         const int smem = WMap<S, R, true>::bytes + 128;

@@ -18,6 +18,7 @@
 // The first 2R planes of a z range arrive in a one-shot warm-up area, whose partial sums are formed in registers.  Every wait is bounded; on any exit path the
 // compute warps meet at a named barrier and warp 0 frees the TMEM.
 #pragma once
+#include <type_traits>
 
 namespace behf {
 namespace tiled {
@@ -25,7 +26,19 @@ namespace tiled {
 #ifndef BEHF_ZQ_NS
 #define BEHF_ZQ_NS 2
 #endif
+// Plane loop unrolled by the stage count, so that each copy's stage (and its shared-memory offsets) is fixed.
+#ifndef BEHF_ZQ_UNROLL
+#define BEHF_ZQ_UNROLL 2
+#endif
+constexpr int kZqUnroll = BEHF_ZQ_UNROLL;
 constexpr uint32_t kZqCols = 128;  // TMEM columns per CTA
+
+// Store a cell pair; FULL: both cells are known to be updated (no per-cell guard).
+template <class S, bool FULL>
+__device__ __forceinline__ void store_cells(S* dst, typename Pair<S>::T v, bool a0, bool a1) {
+    if constexpr (FULL) *reinterpret_cast<typename Pair<S>::T*>(dst) = v;
+    else store_pair<S>(dst, v, a0, a1);
+}
 __device__ __forceinline__ void tm_alloc(uint32_t* dst) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
                  "r"(kZqCols)
@@ -167,7 +180,7 @@ __device__ __forceinline__ void zq_produce(unsigned char* smem, uint64_t* full, 
 }
 
 // ----------------------------------------------------------------------------------------- velocity
-template <class S, int R>
+template <class S, int R, bool SRND>
 __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     k_vel_zq(const __grid_constant__ VMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
     typedef Pair<S> PS;
@@ -231,7 +244,9 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
     const int oe = ty * TXC + xl;
-    const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x2545f491u) : 0u;
+    const uint32_t seed = SRND ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x2545f491u) : 0u;
+    // every lane of the warp updates both of its cells (the interior of the grid): stores need no per-cell guard
+    const bool wfull = __all_sync(0xffffffffu, live && a0 && a1);
     const uint32_t ta = tbase + ((uint32_t)(32 * (ty & 3)) << 16) + (uint32_t)(ty >> 2) * 64u;
     // x and y of a thread are fixed: whether its cells lie in an x or y slab is decided once, z per plane
     const bool xy_slab = g.W > 0 && live && ((a0 && slab_index(x, g.nx, g.L) >= 0) ||
@@ -264,6 +279,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         zq_warm<R, FWD3>(ta + 48, v);
     }
 
+#pragma unroll kZqUnroll
     for (int k = kb, it = 0; k < ke && !failed; k++, it++) {
         const int st = it % NS;
         const bool ok = mbar_wait(&bfull[st], (it / NS) & 1);
@@ -318,6 +334,8 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 const KP kv = *reinterpret_cast<const KP*>(b + M::own_k + j * M::OK + oe * sizeof(K));
                 return mul2(Pair<K>::f2(kv), f2(g.kmulf[kidx], g.kmulf[kidx]));
             };
+            // two copies of the update: warps whose cells are all inside the updated region store unguarded
+            auto update = [&](auto full) {
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 const float2 vw1 = *reinterpret_cast<const float2*>(b + M::own_w + a * M::OWW + oe * 4);
@@ -329,16 +347,19 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 // q' = VW1 q - VW2 sum(d sigma) - VW3 d p
                 const float2 t = fma2(vw2, sum[a], mul2(vw3p, dp[a]));
                 const float2 qn = fma2(vw1, qo, make_float2(-t.x, -t.y));
-                const P qs = g.sr ? SR<S>::pack(qn, mix32(seed ^ (uint32_t)go ^ (0x3c6ef372u * (uint32_t)(a + 1))))
+                const P qs = SRND ? SR<S>::pack(qn, mix32(seed ^ (uint32_t)go ^ (0x3c6ef372u * (uint32_t)(a + 1))))
                                   : PS::pack(qn);
-                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_QX + a]) + go, qs, a0, a1);
+                store_cells<S, decltype(full)::value>(reinterpret_cast<S*>(p.f[BEHF_QX + a]) + go, qs, a0, a1);
                 // v' = v + VU1 sum(d sigma) - VU2 (q' - q)
                 const float2 dq = sub2(PS::f2(qs), qo);
                 const float2 vn = fma2(vu1, sum[a], fma2(make_float2(-vu2.x, -vu2.y), dq, own(a)));
-                const P vs = g.sr ? SR<S>::pack(vn, mix32(seed ^ (uint32_t)go ^ (0x1b873593u * (uint32_t)(a + 1))))
+                const P vs = SRND ? SR<S>::pack(vn, mix32(seed ^ (uint32_t)go ^ (0x1b873593u * (uint32_t)(a + 1))))
                                   : PS::pack(vn);
-                store_pair<S>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, vs, a0, a1);
+                store_cells<S, decltype(full)::value>(reinterpret_cast<S*>(p.f[BEHF_VX + a]) + go, vs, a0, a1);
             }
+            };
+            if (wfull) update(std::true_type{});
+            else update(std::false_type{});
         }
         __syncwarp();
         if (tx == 0) mbar_arrive(&bempty[st]);
@@ -353,7 +374,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 }
 
 // ----------------------------------------------------------------------------------------- stress
-template <class S, int R>
+template <class S, int R, bool SRND>
 __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     k_str_zq(const __grid_constant__ TMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
     typedef Pair<S> PS;
@@ -414,7 +435,8 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     const bool live = (y >= R && y < g.ny - R) && (a0 || a1);
     const long long col = (long long)y * g.px + x;
     const int oe = ty * TXC + xl;
-    const uint32_t seed = g.sr ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x6a09e667u) : 0u;
+    const uint32_t seed = SRND ? mix32((uint32_t)(*g.step + g.step_off) * 0x9e3779b9u + 0x6a09e667u) : 0u;
+    const bool wfull = __all_sync(0xffffffffu, live && a0 && a1);
     const uint32_t ta = tbase + ((uint32_t)(32 * (ty & 3)) << 16) + (uint32_t)(ty >> 2) * 64u;
     const bool xy_slab = g.W > 0 && live && ((a0 && slab_index(x, g.nx, g.L) >= 0) ||
                                              (a1 && slab_index(x + 1, g.nx, g.L) >= 0) || slab_index(y, g.ny, g.L) >= 0);
@@ -446,6 +468,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         zq_warm<R, FWD3>(ta + 48, v);
     }
 
+#pragma unroll kZqUnroll
     for (int k = kb, it = 0; k < ke && !failed; k++, it++) {
         const int st = it % NS;
         const bool ok = mbar_wait(&bfull[st], (it / NS) & 1);
@@ -500,10 +523,12 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 return mul2(Pair<K>::f2(kv), f2(g.kmulf[j], g.kmulf[j]));
             };
             auto own = [&](int q) { return PS::f2(*reinterpret_cast<const P*>(b + M::own_f + q * M::OW + oe * sizeof(S))); };
+            // two copies of the update: warps whose cells are all inside the updated region store unguarded
+            auto update = [&](auto full) {
             auto put = [&](int field, float2 v) {
-                const P sv = g.sr ? SR<S>::pack(v, mix32(seed ^ (uint32_t)go ^ (0x85ebca6bu * (uint32_t)(field + 1))))
+                const P sv = SRND ? SR<S>::pack(v, mix32(seed ^ (uint32_t)go ^ (0x85ebca6bu * (uint32_t)(field + 1))))
                                   : PS::pack(v);
-                store_pair<S>(reinterpret_cast<S*>(p.f[field]) + go, sv, a0, a1);
+                store_cells<S, decltype(full)::value>(reinterpret_cast<S*>(p.f[field]) + go, sv, a0, a1);
             };
             const float2 p1 = kc(0), p2 = kc(1), g1 = kc(2), g2 = kc(3);
             const float2 g3dq = mul2(mul2(p1, f2(g.c_s3, g.c_s3)), dq);  // S3 = P1 c_s3
@@ -514,6 +539,9 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             put(BEHF_SXY, fma2(kc(4), add2(uxy, uyx), own(3)));
             put(BEHF_SXZ, fma2(kc(5), add2(uxz, uzx), own(4)));
             put(BEHF_SYZ, fma2(kc(6), add2(uyz, uzy), own(5)));
+            };
+            if (wfull) update(std::true_type{});
+            else update(std::false_type{});
         }
         __syncwarp();
         if (tx == 0) mbar_arrive(&bempty[st]);
