@@ -39,11 +39,13 @@ import numpy as np  # noqa: E402
 METRIC = "Gpt-updates/s (1024^3 FP16 BEHF, seis relL2<=2e-2)"
 UNIT = "Gpt/s"
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the tiled radius-4 FP16
-# kernels on this workload at 1024^3, from one ncu capture (one pass per launch), per updated cell; the
-# bench multiplies by the cells of its own grid.
-NCU_BYTES_PER_CELL = {("f16", "velocity"): 82.01, ("f16", "stress"): 66.68}
-NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1024^3 launch, per cell x cells"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per updated cell of one launch of the radius-4 FP16
+# tensor-memory kernels, from an ncu capture of a 384^3 grid with a 7-cell CPML (the same slab fraction of the grid
+# as 20 cells at 1024^3; one kernel and two launches per capture, 5 GB on the device); the bench multiplies by the
+# cells of its own grid.
+NCU_BYTES_PER_CELL = {("f16", "tmem", "velocity"): 84.57, ("f16", "tmem", "stress"): 68.47}
+NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per cell of one 384^3 launch with a 7-cell CPML "
+              "(profiles/traffic_k_vel_zq_k_str_zq_random384_f16.md), x cells")
 
 
 def parse():
@@ -331,7 +333,8 @@ def behf_arm(args, world, rank, local):
     peak, peak_kind = peak_hbm()
     achieved = ab[dom] * cells / (kt[dom] * 1e-3) / 1e9
     info = s.info()
-    bpc = NCU_BYTES_PER_CELL.get((args.precision, dom)) if info["kernel"] == "tiled" and prob.radius == 4 else None
+    bpc = (NCU_BYTES_PER_CELL.get((args.precision, info["tiled_variant"], dom))
+           if info["kernel"] == "tiled" and prob.radius == 4 else None)
     traffic = bpc * cells if bpc is not None else None
     traffic_src = NCU_SOURCE if bpc is not None else None
 
