@@ -85,6 +85,7 @@ __device__ __forceinline__ void setc(float2& v, int c, float x) {
 }
 __device__ __forceinline__ float prof(const void* a, int i) { return reinterpret_cast<const float*>(a)[i]; }
 
+
 // CPML of the four derivatives of one axis for one cell: all eight loads first, then the updates, then the
 // eight stores (the arrays cannot alias, but the compiler cannot know; batching keeps one memory latency).
 __device__ __forceinline__ void pml4(const DevPtrs& p, int ax, int slot0, long long so, float A, float B, float A2,
@@ -122,55 +123,135 @@ __device__ __forceinline__ void pml4(const DevPtrs& p, int ax, int slot0, long l
 }
 
 // CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
-// velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.
-template <int SLOT0>
+// velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.  PAIRED: the
+// two cells' memory loads of an axis batched (pml4x2: one memory latency per axis); else cell by cell (pml4: fewer
+// live registers, for kernels at their register limit).  Both give the same bits.
+// CPML of the four derivatives of one axis for both cells of a pair (in[c]: cell c lies in the slab, at element
+// so[c] of the axis' memory arrays): all sixteen loads first, then the updates, then the stores.  The arrays cannot
+// alias, but the compiler cannot know; batching the pair's loads keeps one memory latency per axis instead of one
+// per cell.
+__device__ __forceinline__ void pml4x2(const DevPtrs& p, int ax, int slot0, const long long (&so)[2],
+                                       const bool (&in)[2], float2 A, float2 B, float2 A2, float2 B2, float2& d0,
+                                       float2& d1, float2& d2, float2& d3, bool half0, bool half1, bool half2,
+                                       bool half3) {
+    float s[2][4], v[2][4];
+#pragma unroll
+    for (int c = 0; c < 2; c++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            s[c][j] = in[c] ? reinterpret_cast<const float*>(p.psi[ax][slot0 + j])[so[c]] : 0.f;
+            v[c][j] = in[c] ? reinterpret_cast<const float*>(p.prv[ax][slot0 + j])[so[c]] : 0.f;
+        }
+    float2* d[4] = {&d0, &d1, &d2, &d3};
+    const bool h[4] = {half0, half1, half2, half3};
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        if (!in[c]) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float a = h[j] ? comp(A2, c) : comp(A, c), b = h[j] ? comp(B2, c) : comp(B, c);
+            const float D = comp(*d[j], c);
+            const float pn = a * s[c][j] + b * (a * v[c][j] + D);  // psi = A psi + B (A prev + D)
+            s[c][j] = pn;
+            v[c][j] = D;
+            setc(*d[j], c, D + pn);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        if (!in[c]) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            reinterpret_cast<float*>(p.psi[ax][slot0 + j])[so[c]] = s[c][j];
+            reinterpret_cast<float*>(p.prv[ax][slot0 + j])[so[c]] = v[c][j];
+        }
+    }
+}
+
+// CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
+// velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.  PAIRED: the
+// two cells' memory loads of an axis batched (pml4x2: one memory latency per axis); else cell by cell (pml4: fewer
+// live registers, for kernels at their register limit).  Both give the same bits.
+template <int SLOT0, bool PAIRED>
 __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x, int y, int k, bool a0, bool a1,
                                          float2& dx0, float2& dx1, float2& dx2, float2& dx3, const bool hx[4],
                                          float2& dy0, float2& dy1, float2& dy2, float2& dy3, const bool hy[4],
                                          float2& dz0, float2& dz1, float2& dz2, float2& dz3, const bool hz[4]) {
-#pragma unroll
-    for (int c = 0; c < 2; c++) {
-        const int xc = x + c;
-        const int si = (c ? a1 : a0) ? slab_index(xc, g.nx, g.L) : -1;
-        if (si >= 0) {
-            const long long so = ((long long)k * g.ny + y) * g.W + si;
-            float a = comp(dx0, c), b = comp(dx1, c), d = comp(dx2, c), e = comp(dx3, c);
-            pml4(p, 0, SLOT0, so, prof(p.pa[0], xc), prof(p.pb[0], xc), prof(p.pa2[0], xc), prof(p.pb2[0], xc), a, b,
-                 d, e, hx[0], hx[1], hx[2], hx[3]);
-            setc(dx0, c, a);
-            setc(dx1, c, b);
-            setc(dx2, c, d);
-            setc(dx3, c, e);
+    if constexpr (PAIRED) {
+        {
+            const int si0 = a0 ? slab_index(x, g.nx, g.L) : -1, si1 = a1 ? slab_index(x + 1, g.nx, g.L) : -1;
+            if (si0 >= 0 || si1 >= 0) {
+                const bool in[2] = {si0 >= 0, si1 >= 0};
+                const long long row = ((long long)k * g.ny + y) * g.W;
+                const long long so[2] = {row + si0, row + si1};
+                auto pr = [&](void* const* t) {
+                    return f2(in[0] ? prof(t[0], x) : 0.f, in[1] ? prof(t[0], x + 1) : 0.f);
+                };
+                pml4x2(p, 0, SLOT0, so, in, pr(p.pa), pr(p.pb), pr(p.pa2), pr(p.pb2), dx0, dx1, dx2, dx3, hx[0], hx[1],
+                       hx[2], hx[3]);
+            }
         }
-    }
-    const int sj = slab_index(y, g.ny, g.L);
-    if (sj >= 0) {
-        const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
+        const int sj = slab_index(y, g.ny, g.L);
+        if (sj >= 0) {
+            const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
+            const bool in[2] = {a0, a1};
+            const long long so[2] = {((long long)k * g.W + sj) * g.nx + x, ((long long)k * g.W + sj) * g.nx + x + 1};
+            pml4x2(p, 1, SLOT0, so, in, f2(A, A), f2(B, B), f2(A2, A2), f2(B2, B2), dy0, dy1, dy2, dy3, hy[0], hy[1],
+                   hy[2], hy[3]);
+        }
+        const int sk = slab_index(k, g.nz, g.L);
+        if (sk >= 0) {
+            const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
+            const bool in[2] = {a0, a1};
+            const long long so[2] = {((long long)sk * g.ny + y) * g.nx + x, ((long long)sk * g.ny + y) * g.nx + x + 1};
+            pml4x2(p, 2, SLOT0, so, in, f2(A, A), f2(B, B), f2(A2, A2), f2(B2, B2), dz0, dz1, dz2, dz3, hz[0], hz[1],
+                   hz[2], hz[3]);
+        }
+    } else {
 #pragma unroll
         for (int c = 0; c < 2; c++) {
-            if (!(c ? a1 : a0)) continue;
-            const long long so = ((long long)k * g.W + sj) * g.nx + x + c;
-            float a = comp(dy0, c), b = comp(dy1, c), d = comp(dy2, c), e = comp(dy3, c);
-            pml4(p, 1, SLOT0, so, A, B, A2, B2, a, b, d, e, hy[0], hy[1], hy[2], hy[3]);
-            setc(dy0, c, a);
-            setc(dy1, c, b);
-            setc(dy2, c, d);
-            setc(dy3, c, e);
+            const int xc = x + c;
+            const int si = (c ? a1 : a0) ? slab_index(xc, g.nx, g.L) : -1;
+            if (si >= 0) {
+                const long long so = ((long long)k * g.ny + y) * g.W + si;
+                float a = comp(dx0, c), b = comp(dx1, c), d = comp(dx2, c), e = comp(dx3, c);
+                pml4(p, 0, SLOT0, so, prof(p.pa[0], xc), prof(p.pb[0], xc), prof(p.pa2[0], xc), prof(p.pb2[0], xc), a, b,
+                     d, e, hx[0], hx[1], hx[2], hx[3]);
+                setc(dx0, c, a);
+                setc(dx1, c, b);
+                setc(dx2, c, d);
+                setc(dx3, c, e);
+            }
         }
-    }
-    const int sk = slab_index(k, g.nz, g.L);
-    if (sk >= 0) {
-        const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
+        const int sj = slab_index(y, g.ny, g.L);
+        if (sj >= 0) {
+            const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
-            if (!(c ? a1 : a0)) continue;
-            const long long so = ((long long)sk * g.ny + y) * g.nx + x + c;
-            float a = comp(dz0, c), b = comp(dz1, c), d = comp(dz2, c), e = comp(dz3, c);
-            pml4(p, 2, SLOT0, so, A, B, A2, B2, a, b, d, e, hz[0], hz[1], hz[2], hz[3]);
-            setc(dz0, c, a);
-            setc(dz1, c, b);
-            setc(dz2, c, d);
-            setc(dz3, c, e);
+            for (int c = 0; c < 2; c++) {
+                if (!(c ? a1 : a0)) continue;
+                const long long so = ((long long)k * g.W + sj) * g.nx + x + c;
+                float a = comp(dy0, c), b = comp(dy1, c), d = comp(dy2, c), e = comp(dy3, c);
+                pml4(p, 1, SLOT0, so, A, B, A2, B2, a, b, d, e, hy[0], hy[1], hy[2], hy[3]);
+                setc(dy0, c, a);
+                setc(dy1, c, b);
+                setc(dy2, c, d);
+                setc(dy3, c, e);
+            }
+        }
+        const int sk = slab_index(k, g.nz, g.L);
+        if (sk >= 0) {
+            const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                if (!(c ? a1 : a0)) continue;
+                const long long so = ((long long)sk * g.ny + y) * g.nx + x + c;
+                float a = comp(dz0, c), b = comp(dz1, c), d = comp(dz2, c), e = comp(dz3, c);
+                pml4(p, 2, SLOT0, so, A, B, A2, B2, a, b, d, e, hz[0], hz[1], hz[2], hz[3]);
+                setc(dz0, c, a);
+                setc(dz1, c, b);
+                setc(dz2, c, d);
+                setc(dz3, c, e);
+            }
         }
     }
 }
@@ -383,7 +464,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB)
                 // x: x1 (fwd), s1 (fwd), y2 (bwd), z2 (bwd); y: y1, s2 (fwd), x2, z3 (bwd);
                 // z: z1, s3 (fwd), x3, y3 (bwd)
                 const bool hf[4] = {true, true, false, false};
-                pml_pair<0>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
+                pml_pair<0, sizeof(S) == 4>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
@@ -558,7 +639,7 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
             if (g.W > 0) {
                 // x: uxx, wx (bwd), uyx, uzx (fwd); y: uyy, wy (bwd), uxy, uzy (fwd); z: uzz, wz (bwd), uxz, uyz (fwd)
                 const bool hf[4] = {false, false, true, true};
-                pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
+                pml_pair<4, sizeof(S) == 4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
             }
             if (smode == 1) load_fields();
             if (smode != 0) load_coefs();

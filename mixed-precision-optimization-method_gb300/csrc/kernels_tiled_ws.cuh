@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             float2 y3 = col_bwd<R>(cv);
             if (g.W > 0) {
                 const bool hf[4] = {true, true, false, false};
-                pml_pair<0>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
+                pml_pair<0, true>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             float2 uyz = col_fwd<R>(cv);
             if (g.W > 0) {
                 const bool hf[4] = {false, false, true, true};
-                pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
+                pml_pair<4, true>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);

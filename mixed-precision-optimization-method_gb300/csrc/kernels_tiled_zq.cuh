@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             const long long go = (long long)k * g.plane + col;
             if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
                 const bool hf[4] = {true, true, false, false};
-                pml_pair<0>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
+                pml_pair<0, false>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             const long long go = (long long)k * g.plane + col;
             if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
                 const bool hf[4] = {false, false, true, true};
-                pml_pair<4>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
+                pml_pair<4, false>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);
