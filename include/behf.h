@@ -118,6 +118,11 @@ enum {
                                     accumulators sum each checkpoint segment in FP32, then fold it into running
                                     totals: 1 = Neumaier-compensated FP32 totals (default), 0 = no fold (plain FP32
                                     accumulation over all steps), 2 = FP64 totals (reference for the error) */
+    BEHF_OPT_RECOMPUTE_OVERLAP = 12, /* gradient, one checkpoint level: 1 = the recompute of the next segment from its
+                                    checkpoint runs on a second stream, into a second snapshot buffer, while the
+                                    current segment's adjoint steps run (default; only when the second buffer fits
+                                    the free device memory less max(2 GiB, 2 %)), 0 = one after the other.  The
+                                    results are the same bit for bit. */
 };
 
 /* Create a context; allocates the wavefields, coefficients and CPML slab memory on the current

@@ -24,7 +24,8 @@ PRECISION = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
 (OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
- OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER, OPT_TILED_VARIANT, OPT_GRAD_COMPENSATION) = range(12)
+ OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER, OPT_TILED_VARIANT, OPT_GRAD_COMPENSATION,
+ OPT_RECOMPUTE_OVERLAP) = range(13)
 TILED_VARIANT = {"auto": 0, "classic": 1, "ws": 2, "tmem": 3}
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
@@ -299,16 +300,19 @@ class Solver:
         return int(self._lib.behf_selftest_wait(self._ctx))
 
     # -- gradient (adjoint state, checkpointed)
-    def enable_gradient(self, checkpoint: int = 0, snapshot_cache: int = -1, checkpoint_outer: int = 0):
+    def enable_gradient(self, checkpoint: int = 0, snapshot_cache: int = -1, checkpoint_outer: int = 0,
+                        overlap: int = 1):
         """Keep the moduli on the device for behf_gradient (call before the medium); checkpoint = steps
         between checkpoints of the gradient's forward pass (0 = round(sqrt(nt))); snapshot_cache = device MiB
         for keeping the forward pass's snapshots of the last segments (-1 automatic, 0 none: every segment is
         recomputed from its checkpoint); checkpoint_outer = outer spacing of the two-level scheme (0 automatic:
-        two levels only when one does not fit the device memory)."""
+        two levels only when one does not fit the device memory); overlap = 1: a segment's recompute runs on a
+        second stream while the previous segment's adjoint steps run (0: one after the other)."""
         self.set_option(OPT_GRADIENT, 1)
         self.set_option(OPT_CHECKPOINT, int(checkpoint))
         self.set_option(OPT_SNAPSHOT_CACHE, int(snapshot_cache))
         self.set_option(OPT_CHECKPOINT_OUTER, int(checkpoint_outer))
+        self.set_option(OPT_RECOMPUTE_OVERLAP, int(overlap))
 
     def _grad_out(self, nt, moduli):
         gw = np.zeros(nt, np.float64)
@@ -410,7 +414,8 @@ def run_batch(solvers, nsteps: int):
 
 
 def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None, gradient=False,
-               checkpoint=0, coef_rounding=0, state_rounding=0, snapshot_cache=-1, checkpoint_outer=0) -> Solver:
+               checkpoint=0, coef_rounding=0, state_rounding=0, snapshot_cache=-1, checkpoint_outer=0,
+               overlap=1) -> Solver:
     """A Solver set up with a problem description (see behf.problems.Problem); gradient=True keeps what
     Solver.gradient needs."""
     s = Solver(prob.nx, prob.ny, prob.nz, prob.h, prob.dt, radius=prob.radius, precision=precision,
@@ -421,7 +426,7 @@ def solver_for(prob, precision="f16", kernel="auto", scales=None, capacity=None,
         s.set_option(OPT_REF_BUG_COMPAT, 1)
     s.set_kernel(kernel)
     if gradient:
-        s.enable_gradient(checkpoint, snapshot_cache, checkpoint_outer)
+        s.enable_gradient(checkpoint, snapshot_cache, checkpoint_outer, overlap)
     if coef_rounding:
         s.set_option(OPT_COEF_ROUNDING, int(coef_rounding))
     if state_rounding:

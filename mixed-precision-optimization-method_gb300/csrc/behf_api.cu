@@ -2,6 +2,7 @@
 // graph-captured time loop.  Replaces the reference's host/device boundary: main.cpp:1529-1743
 // (allocation and copies of the blockInfo arrays) and callCUDAKernel (kernel.cu:1728-2698).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstdarg>
@@ -138,6 +139,7 @@ struct behf_ctx {
     int ck_outer = 0;  // gradient: outer checkpoint spacing of the two-level scheme (0 automatic)
     int snap_cache_mib = -1;  // gradient: device memory for snapshots kept from the forward pass (-1 automatic)
     int grad_comp = 1;    // gradient: FP32 accumulators folded per segment (0 plain, 1 Neumaier, 2 FP64 total)
+    int rc_overlap = 1;   // gradient: recompute of the next segment on a second stream (one checkpoint level)
     int coef_dither = 0;  // BEHF_OPT_COEF_ROUNDING
 
     ~behf_ctx() {
@@ -932,6 +934,10 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0 || value > 2) return fail(BEHF_ERR_INVALID, "gradient compensation must be 0, 1 or 2");
             c->grad_comp = value;
             break;
+        case BEHF_OPT_RECOMPUTE_OVERLAP:
+            if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "recompute overlap must be 0 or 1");
+            c->rc_overlap = value;
+            break;
         case BEHF_OPT_TILED_VARIANT:
             if (value < 0 || value > 3) return fail(BEHF_ERR_INVALID, "tiled variant must be 0, 1, 2 or 3");
             c->g.ws = value == 0 ? auto_variant(c->prec) : value - 1;
@@ -1188,6 +1194,25 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     // (BEHF_OPT_SNAPSHOT_CACHE: -1 all of it but max(8 GiB, 10 %), 0 none, else that many MiB); their slot 0 is the
     // segment's checkpoint, which holds the 13 fields in the same layout.  The others share one buffer.
     std::vector<char*> cache(nseg, nullptr);
+    // Overlap (one level): segment sg - 1 is recomputed on a second stream, into the other of two snapshot buffers
+    // (segment parity), while segment sg runs its adjoint steps.  The adjoint reads only the coefficients, the CPML
+    // profiles and the snapshots, never the forward state the recompute overwrites; events order each buffer's
+    // reuse.  The second buffer is allocated only when some segment will be recomputed and it fits.
+    char* snap2 = nullptr;
+    {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const size_t cmargin = std::max((size_t)8 << 30, tot / 10);
+        size_t budget = fr > cmargin ? fr - cmargin : 0;
+        if (c->snap_cache_mib > 0) budget = std::min(budget, (size_t)c->snap_cache_mib << 20);
+        const bool all_cached = c->snap_cache_mib != 0 && budget / (snap_bytes * (size_t)S_) >= (size_t)nseg;
+        const size_t need = snap_bytes * (S_ + 1), margin = std::max((size_t)2 << 30, tot / 50);
+        if (c->rc_overlap && !two && nseg > 1 && !all_cached && fr > need + margin) {
+            st = buf.get((void**)&snap2, need);
+            if (st) return st;
+        }
+    }
+    const bool overlap = snap2 != nullptr;
     if (c->snap_cache_mib != 0 && !two) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
@@ -1203,17 +1228,19 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             }
     }
     auto cached = [&](int sg) { return sg >= 0 && cache[sg] != nullptr; };  // sg -1: a segment never cached
+    // the recompute buffer of an uncached segment: the shared one, or with overlap the one of the segment's parity
+    auto rbuf = [&](int sg) { return overlap && (sg & 1) ? 1 : 0; };
     auto snap_ptr = [&](int sg, int idx, int f) -> char* {
         const size_t fo = align256(nf * c->es) * f;
         if (cached(sg)) return idx == 0 ? ck + ck_bytes * sg + fo : cache[sg] + snap_bytes * (idx - 1) + fo;
-        return snap + snap_bytes * idx + fo;
+        return (rbuf(sg) ? snap2 : snap) + snap_bytes * idx + fo;
     };
     // tensor maps of a segment's snapshot slots (the 16-bit kinds stage snapshot windows in the gathers)
     std::vector<GatherMaps> snap_mt, snap_mv;
-    int maps_seg = -2;  // segment whose buffers the maps describe (-1: the shared buffer)
+    int maps_seg = INT_MIN;  // segment whose buffers the maps describe (-1 / -2: the first / second shared buffer)
     auto build_snap_maps = [&](int sg) -> cudaError_t {
         if (!adj_snap_staged<S>()) return cudaSuccess;
-        const int key = cached(sg) ? sg : -1;
+        const int key = cached(sg) ? sg : -1 - rbuf(sg);
         if (key == maps_seg) return cudaSuccess;
         snap_mt.resize(S_ + 1);
         snap_mv.resize(S_ + 1);
@@ -1279,6 +1306,53 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
         return aux_tick(c->d_it, 1, c->stream);
     };
 
+    // recompute a segment from its checkpoint on c->stream, keeping the fields after V (+ force) of every step
+    auto recompute = [&](int sg, int s0, int s1, char* ckp) -> cudaError_t {
+        cudaError_t e;
+        if ((e = copy_state(ckp, false)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(c->d_it, 0, sizeof(int), c->stream)) != cudaSuccess) return e;
+        if (s0 > 0 && (e = aux_tick(c->d_it, s0, c->stream)) != cudaSuccess) return e;
+        if ((e = snap_fields(sg, 0)) != cudaSuccess) return e;
+        for (int it = s0; it < s1; it++)
+            if ((e = snap_step(sg, it - s0 + 1, false)) != cudaSuccess) return e;
+        return cudaSuccess;
+    };
+    // the second stream of the overlap and its events (done: a buffer's recompute finished; free: the adjoint
+    // steps that read a buffer finished); destroyed, after its work, before the buffers are freed
+    struct Side {
+        cudaStream_t s = nullptr;
+        cudaEvent_t done[2] = {}, free[2] = {};
+        ~Side() {
+            if (s) cudaStreamSynchronize(s);
+            for (int i = 0; i < 2; i++) {
+                if (done[i]) cudaEventDestroy(done[i]);
+                if (free[i]) cudaEventDestroy(free[i]);
+            }
+            if (s) cudaStreamDestroy(s);
+        }
+    } side;
+    if (overlap) {
+        CK(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++) {
+            CK(cudaEventCreateWithFlags(&side.done[i], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&side.free[i], cudaEventDisableTiming));
+        }
+    }
+    int prefetched = -1;  // the last segment whose recompute was enqueued on the second stream
+    auto recompute_on_side = [&](int sg) -> cudaError_t {
+        const int s0 = sg * S_, s1 = std::min(nt, s0 + S_);
+        const int b = rbuf(sg);
+        cudaError_t e = cudaStreamWaitEvent(side.s, side.free[b], 0);  // the adjoint steps of buffer b's last use
+        if (e != cudaSuccess) return e;
+        cudaStream_t main = c->stream;
+        c->stream = side.s;
+        e = recompute(sg, s0, s1, ck + ck_bytes * sg);
+        c->stream = main;
+        if (e != cudaSuccess) return e;
+        prefetched = sg;
+        return cudaEventRecord(side.done[b], side.s);
+    };
+
     // forward pass with checkpoints (seismograms recorded as in behf_run); cached segments step by step
     st = zero_state(c);
     if (st) return st;
@@ -1339,13 +1413,16 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             const int sg = two ? -1 : og;  // the segment's index in the snapshot cache (never cached with two levels)
             const int s0 = o0 + j * S_, s1 = std::min(o1, s0 + S_);
             char* ckp = two ? ckin + ck_bytes * j : ck + ck_bytes * og;
-            if (!cached(sg)) {  // recompute the segment from its checkpoint, keeping the fields after V (+ force)
-                CK(copy_state(ckp, false));
-                CK(cudaMemcpyAsync(c->d_it, &s0, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-                CK(cudaStreamSynchronize(c->stream));
-                CK(snap_fields(sg, 0));
-                for (int it = s0; it < s1; it++) CK(snap_step(sg, it - s0 + 1, false));
+            if (!cached(sg)) {
+                if (!overlap) {
+                    CK(recompute(sg, s0, s1, ckp));
+                } else {
+                    if (prefetched != sg) CK(recompute_on_side(sg));  // the first recomputed segment
+                    CK(cudaStreamWaitEvent(c->stream, side.done[rbuf(sg)], 0));
+                }
             }
+            // the next segment's recompute, on the second stream, while this one runs its adjoint steps
+            if (overlap && sg >= 1 && !cached(sg - 1)) CK(recompute_on_side(sg - 1));
             CK(build_snap_maps(sg));
             // backward step it: T^T per cell of it is done (the first step: here, after its record^T; later steps:
             // fused into the V^T gather of step it + 1, completed by the record^T of it)
@@ -1372,6 +1449,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                 CK(adj_fold(fold, (long long)nf, 0, c->stream));
                 c->launches++;
             }
+            if (overlap && !cached(sg)) CK(cudaEventRecord(side.free[rbuf(sg)], c->stream));
         }
     }
     if (folding) {

@@ -2,7 +2,7 @@
 FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identity and finite differences):
   * FP64: wavelet and moduli gradients within 1e-9 relative L2 of the oracle, every source kind, radius 1/2/4,
     with and without CPML; dot-product identity within 1e-10; checkpoint spacing, two checkpoint levels and the
-    snapshot cache change nothing;
+    snapshot cache and the overlap of the recompute with the adjoint steps change nothing;
   * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
   * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
 from __future__ import annotations
@@ -32,9 +32,9 @@ def rel(a, b):
     return np.linalg.norm((a - b).ravel()) / d if d > 0 else np.linalg.norm(a.ravel())
 
 
-def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto", snapshot_cache=-1, checkpoint_outer=0):
+def gpu_gradient(p, adj, precision, checkpoint=0, kernel="auto", snapshot_cache=-1, checkpoint_outer=0, overlap=1):
     s = behf.solver_for(p, precision=precision, kernel=kernel, gradient=True, checkpoint=checkpoint,
-                        snapshot_cache=snapshot_cache, checkpoint_outer=checkpoint_outer)
+                        snapshot_cache=snapshot_cache, checkpoint_outer=checkpoint_outer, overlap=overlap)
     gw, gm = s.gradient(p.nt, adj)
     seis = s.seismograms()
     s.close()
@@ -86,14 +86,18 @@ def test_gradient_checkpoint_spacing(behf_lib):
 @pytest.mark.parametrize("precision", ["f64", "f16"])
 def test_gradient_snapshot_cache(behf_lib, precision):
     # every segment recomputed (0), the last two kept from the forward pass (50 MiB of 1.6 MB slots x 13 per
-    # segment at f64), all kept (-1): the same gradient, bit for bit
+    # segment at f64), all kept (-1): the same gradient, bit for bit; and the recomputes overlapped with the
+    # adjoint steps on a second stream (the default) or run one after the other
     p = small(R=2, L=4)
     adj = np.random.default_rng(7).standard_normal((len(p.rec_comp), p.nt))
-    ref = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=0)
-    for cache in (50, -1):
-        out = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=cache)
-        for a, b in zip(out, ref):
-            np.testing.assert_array_equal(a, b)
+    ref = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=0, overlap=0)
+    for cache in (0, 50, -1):
+        for overlap in (0, 1):
+            if (cache, overlap) == (0, 0):
+                continue
+            out = gpu_gradient(p, adj, precision, checkpoint=13, snapshot_cache=cache, overlap=overlap)
+            for a, b in zip(out, ref):
+                np.testing.assert_array_equal(a, b)
     # two checkpoint levels (outer segments of 39 = 3 x 13 steps, each run again for its inner checkpoints)
     out = gpu_gradient(p, adj, precision, checkpoint=13, checkpoint_outer=30)
     for a, b in zip(out, ref):
