@@ -284,7 +284,7 @@ def shots_leg(args):
             group = [behf.solver_for(shots.shot_problem(n, 1000 * n + i, nt), precision=args.precision)
                      for i in range(g0, min(per, g0 + batch))]
             for s in group:
-                s.set_option(behf.OPT_TILED_VARIANT, {"classic": 1, "ws": 2, "tmem": 3}[tuned[n]["variant"]])
+                s.set_option(behf.OPT_TILED_VARIANT, behf.TILED_VARIANT[tuned[n]["variant"]])
                 s.set_option(behf.OPT_ZCHUNK, tuned[n]["zchunk"])
             l0 = sum(s.info()["launches"] for s in group)
             torch.cuda.synchronize()

@@ -80,7 +80,8 @@ typedef struct {
     int kernel;              /* kernel family in use (behf_kernel) */
     int radius, precision;
     int64_t launches;        /* kernels enqueued by this context so far (graph launches count their nodes) */
-    int tiled_variant;       /* tiled kernels in use: 1 classic, 2 warp-specialised, 3 warp-specialised + TMEM z */
+    int tiled_variant;       /* tiled kernels in use: 1 classic, 2 warp-specialised, 3 warp-specialised + TMEM z,
+                                4 the same + x-slab CPML memory by TMA */
     int zchunk;              /* z planes per CTA requested for the tiled kernels (0 = automatic) */
 } behf_info;
 
@@ -110,10 +111,12 @@ enum {
     BEHF_OPT_CHECKPOINT_OUTER = 9, /* gradient: outer checkpoint spacing of the two-level scheme, rounded up to a
                                     multiple of BEHF_OPT_CHECKPOINT (0 = automatic: one level when it fits the
                                     device memory, else two levels with the inner spacing halved until they fit) */
-    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic (3 for FP16 / BF16, 2 for FP32), 1 = classic (own-cell data by direct loads of the
+    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic (4 for FP16, 3 for BF16, 2 for FP32), 1 = classic (own-cell data by direct loads of the
                                     compute threads), 2 = warp-specialised (a producer warp brings every input,
                                     own-cell data included, through TMA), 3 = warp-specialised with the z derivatives
-                                    accumulated plane by plane in tensor memory (TMEM) */
+                                    accumulated plane by plane in tensor memory (TMEM), 4 = 3 with the CPML memory
+                                    and damping profiles of the x-edge tiles' slab cells also brought by TMA (as 3
+                                    where an x-edge tile's slab cells do not fit its box) */
     BEHF_OPT_GRAD_COMPENSATION = 11, /* gradient with an FP32 adjoint (16/32-bit kinds): the coefficient-gradient
                                     accumulators sum each checkpoint segment in FP32, then fold it into running
                                     totals: 1 = Neumaier-compensated FP32 totals (default), 0 = no fold (plain FP32
@@ -269,7 +272,7 @@ behf_status behf_physical_gradient(long long ncell, const float* const moduli[BE
                                    double* const grad_phys[BEHF_NPHYS]);
 
 /* Autotuner (no counterpart in the reference, which fixes its 16 x 8 block, kernel.cu:17-19): times trial_steps
- * steps for each tiled-kernel variant (BEHF_OPT_TILED_VARIANT 1..3) and each z-chunk length (BEHF_OPT_ZCHUNK
+ * steps for each tiled-kernel variant (BEHF_OPT_TILED_VARIANT 1..4) and each z-chunk length (BEHF_OPT_ZCHUNK
  * candidates 0, 16, 32, ... up to the grid), keeps the fastest pair, and resets the wavefields (behf_reset).
  * Writes the chosen z-chunk and its milliseconds per step; the chosen variant is in behf_info.tiled_variant. */
 behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, double* ms_per_step_out);

@@ -26,7 +26,7 @@ KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
 (OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
  OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER, OPT_TILED_VARIANT, OPT_GRAD_COMPENSATION,
  OPT_RECOMPUTE_OVERLAP) = range(13)
-TILED_VARIANT = {"auto": 0, "classic": 1, "ws": 2, "tmem": 3}
+TILED_VARIANT = {"auto": 0, "classic": 1, "ws": 2, "tmem": 3, "tmem_xs": 4}
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
 
@@ -267,7 +267,7 @@ class Solver:
         return {"step": inf.step, "device_bytes": inf.device_bytes, "scales": tuple(inf.scales),
                 "bytes_per_cell": inf.bytes_per_cell, "kernel": {0: "auto", 1: "plain", 2: "tiled"}[inf.kernel],
                 "radius": inf.radius, "precision": inf.precision, "launches": inf.launches,
-                "tiled_variant": {1: "classic", 2: "ws", 3: "tmem"}.get(inf.tiled_variant, "classic"),
+                "tiled_variant": {1: "classic", 2: "ws", 3: "tmem", 4: "tmem_xs"}.get(inf.tiled_variant, "classic"),
                 "zchunk": inf.zchunk}
 
     def update_wavelet(self, it0: int, w: np.ndarray):

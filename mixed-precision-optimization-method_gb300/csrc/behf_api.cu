@@ -27,7 +27,10 @@ thread_local std::string g_err;
 // derivatives in tensor memory for the 16-bit kinds, the warp-specialised kernels for FP32 (1024^3 on one GB300:
 // FP16 30.5 / 33.7 / 35.2, BF16 28.7 / 32.1 / 34.0, FP32 20.8 / 21.7 / 21.2 Gpt/s for classic / warp-specialised /
 // tensor-memory z).
-int auto_variant(int precision) { return precision == BEHF_FP16 || precision == BEHF_BF16 ? 2 : 1; }
+// Automatic tiled-kernel variant (Geom::ws = BEHF_OPT_TILED_VARIANT - 1), the fastest measured at 1024^3: the tensor-
+// memory kernels with the x-slab staging for FP16, without it for BF16 (its stress kernel spills more with it),
+// the warp-specialised kernels for FP32.
+int auto_variant(int precision) { return precision == BEHF_FP16 ? 3 : precision == BEHF_BF16 ? 2 : 1; }
 
 behf_status fail(behf_status code, const char* fmt, ...) {
     char buf[512];
@@ -506,7 +509,10 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.nz = gr->nz;
     g.R = R;
     g.L = L;
-    g.W = L > 0 ? 2 * L + 1 : 0;
+    g.W = L > 0 ? (2 * L + 1 + 3) / 4 * 4 : 0;  // slab row pitch: 2L+1 cells rounded up to 16 bytes of FP32
+    // the tensor-memory kernels' TMA box of x-slab memory: an edge tile's slab cells (at most L + 1, at most a tile
+    // row of 64) plus up to 3 cells of alignment
+    g.xs_bw = L > 0 ? std::min(64, (std::min(L + 1, 64) + 3 + 3) / 4 * 4) : 0;
     g.px = ((long long)gr->nx + 15) / 16 * 16;
     g.plane = g.px * gr->ny;
     g.bug = 0;
@@ -939,7 +945,7 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             c->rc_overlap = value;
             break;
         case BEHF_OPT_TILED_VARIANT:
-            if (value < 0 || value > 3) return fail(BEHF_ERR_INVALID, "tiled variant must be 0, 1, 2 or 3");
+            if (value < 0 || value > 4) return fail(BEHF_ERR_INVALID, "tiled variant must be 0 .. 4");
             c->g.ws = value == 0 ? auto_variant(c->prec) : value - 1;
             break;
         default: return fail(BEHF_ERR_INVALID, "unknown option %d", opt);
@@ -957,7 +963,7 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
     // (8 derivatives x {psi, prev} x read+write) on the slab fraction of each axis
     const double n3[3] = {(double)c->grid.nx, (double)c->grid.ny, (double)c->grid.nz};
     double cpml = 0;
-    for (int a = 0; a < 3; a++) cpml += c->g.W > 0 ? 16.0 * 2.0 * c->ws * c->g.W / n3[a] : 0.0;
+    for (int a = 0; a < 3; a++) cpml += c->g.W > 0 ? 16.0 * 2.0 * c->ws * (2 * c->g.L + 1) / n3[a] : 0.0;
     out->bytes_per_cell = 26.0 * c->es + 3.0 * c->ws + 20.0 * c->ks + cpml;
     out->kernel = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? BEHF_KERNEL_TILED : BEHF_KERNEL_PLAIN;
     out->radius = c->g.R;
@@ -1583,7 +1589,7 @@ behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double*
     // (variant, z chunk) pairs: the variants only where the tiled kernels run
     std::vector<std::pair<int, int>> cand;
     const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok;
-    for (int v = tiled ? 0 : c->g.ws; v <= (tiled ? 2 : c->g.ws); v++)
+    for (int v = tiled ? 0 : c->g.ws; v <= (tiled ? 3 : c->g.ws); v++)
         for (int z : zc) cand.push_back({v, z});
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));

@@ -8,9 +8,10 @@
 //     for FP64) and 20 more in K (half for the 16-bit kinds, else S) multiplied by a power of two
 //     kmul[j] so that each array's largest magnitude sits just below 1.
 //   * CPML memory only inside the boundary slabs: for each axis 8 derivatives x {psi, previous
-//     derivative} in W, slab width W = 2L+1 cells ([0,L) and [n-1-L, n)), layouts
-//     x: [nz][ny][W], y: [nz][W][nx], z: [W][ny][nx].  The reference keeps 24+24 full-volume
-//     FP16 arrays instead (common.h:27-30).
+//     derivative} in W, 2L+1 slab cells ([0,L) and [n-1-L, n)) at slab indices 0..2L, layouts
+//     x: [nz][ny][W], y: [nz][W][nx], z: [W][ny][nx] with W = 2L+1 rounded up to a multiple of 4 (16-byte
+//     rows of FP32 for the tensor-memory kernels' TMA boxes of x-slab memory; the padding is never
+//     touched).  The reference keeps 24+24 full-volume FP16 arrays instead (common.h:27-30).
 //   * 1-D damping profiles per axis (A = e, B = -dt d / 2, and the half-shifted A2, B2).
 #pragma once
 #include <cuda_bf16.h>
@@ -110,7 +111,8 @@ struct DevPtrs {
 
 struct Geom {
     int nx, ny, nz;
-    int R, L, W;           // stencil half-width, CPML width, slab width 2L+1 (0 without CPML)
+    int R, L, W;           // stencil half-width, CPML width, slab pitch (2L+1 rounded up to 4; 0 without CPML)
+    int xs_bw;             // tensor-memory kernels: width of the TMA box of x-slab CPML memory (0: none)
     long long px, plane;   // row pitch and plane stride in elements
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out

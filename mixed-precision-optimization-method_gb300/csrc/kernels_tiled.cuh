@@ -113,11 +113,15 @@ struct VMaps {
     // own-cell boxes of the warp-specialised kernel: vx vy vz qx qy qz, VW1 x y z (FP32), then VW3, VU1, VU2
     // (x y z each)
     CUtensorMap own[18];
+    CUtensorMap xs[8];    // x-slab CPML memory of slots 0..3 (psi 0..3, then prev 0..3): boxes xs_bw x TY x 1
+    CUtensorMap xp[4];    // x damping profiles A, B, A2, B2: 1-D boxes of TXC
 };
 struct TMaps {
     CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
     CUtensorMap zlead[4]; // vx vy vz qz: own-cell boxes for the z ring
     CUtensorMap own[14];  // sxx syy szz sxy sxz syz p, then P1 P2 S1 S2 Sxy Sxz Syz
+    CUtensorMap xs[8];    // x-slab CPML memory of slots 4..7 (psi, then prev)
+    CUtensorMap xp[4];    // x damping profiles A, B, A2, B2
 };
 
 // ------------------------------------------------------------------------------------- PTX helpers
@@ -155,6 +159,12 @@ __device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, uint64_t
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+__device__ __forceinline__ void tma1(void* dst, const CUtensorMap* map, uint64_t* bar, int x) {
+    asm volatile(
+        "cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x)
         : "memory");
 }
 __device__ __forceinline__ void fence_init() {
@@ -280,6 +290,49 @@ inline bool encode(CUtensorMap* m, const Geom& g, void* base, int bw, int bh) {
     return fn(m, dtype_of<T>(), 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// 3-D map over one x-slab CPML memory array ([nz][ny][W] FP32, W a multiple of 4), box bw x TY x 1.
+inline bool encode_xslab(CUtensorMap* m, const Geom& g, void* base, int bw) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.W, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.W * 4, (cuuint64_t)g.W * g.ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)TY, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// 1-D map over an FP32 array of n values (a damping profile), boxes of TXC; beyond n the box reads zeros.
+inline bool encode_prof(CUtensorMap* m, int n, void* base) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[1] = {(cuuint64_t)n};
+    const cuuint64_t strides[1] = {4};  // unused for rank 1
+    const cuuint32_t box[1] = {(cuuint32_t)TXC};
+    const cuuint32_t es[1] = {1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The tile's box of x-slab CPML memory (tensor-memory kernels): the first slab index it starts at, or -1 when the
+// tile updates no x-slab cell, updates cells of both slabs, or its slab cells do not fit a box of g.xs_bw
+// starting at a multiple of 4 (16 bytes, the TMA rule for the innermost coordinate).  CTA-uniform.
+__host__ __device__ __forceinline__ int xs_tile_base(const Geom& g, int x0) {
+    if (g.xs_bw <= 0 || g.W <= 0) return -1;
+    const int lo = x0 > g.R ? x0 : g.R;
+    const int hi = x0 + TXC < g.nx - g.R ? x0 + TXC : g.nx - g.R;  // updated cells [lo, hi)
+    if (lo >= hi) return -1;
+    const int r0 = g.nx - 1 - g.L;  // first cell of the upper slab (slab index L)
+    const bool left = lo < g.L, right = hi > r0;
+    if (left == right) return -1;
+    const int s_lo = left ? lo : g.L + ((lo > r0 ? lo : r0) - r0);
+    const int s_hi = left ? (hi < g.L ? hi : g.L) : g.L + (hi - r0);
+    const int base = s_lo & ~3;
+    return s_hi - base <= g.xs_bw ? base : -1;
 }
 
 // Trapezoidal CPML memory update of one cell: psi = A psi + B (A prev + D); prev = D; returns D + psi.

@@ -125,7 +125,28 @@ __device__ __forceinline__ void pml4(const DevPtrs& p, int ax, int slot0, long l
 // CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
 // velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.  PAIRED: the
 // two cells' memory loads of an axis batched (pml4x2: one memory latency per axis); else cell by cell (pml4: fewer
-// live registers, for kernels at their register limit).  Both give the same bits.
+// live registers, for kernels at their register limit); XS (cell by cell only): the x-slab memory and the x
+// profiles read from shared memory, xrow being this warp's row of a TMA box that starts at slab index xbase (arrays
+// xplane floats apart) and xprof the pair's entry in the tile's profile boxes (A, B, A2, B2, TXC floats apart).
+// All forms give the same bits.
+// The same with the cell's memory already in shared memory (psi of the four slots, then prev, sp floats apart):
+// one derivative at a time, since a shared-memory load needs no batching, so that few registers stay live.
+__device__ __forceinline__ void pml4_sm(const DevPtrs& p, int ax, int slot0, long long so, const float* sm, int sp,
+                                        float A, float B, float A2, float B2, float& d0, float& d1, float& d2,
+                                        float& d3, bool half0, bool half1, bool half2, bool half3) {
+    float* d[4] = {&d0, &d1, &d2, &d3};
+    const bool h[4] = {half0, half1, half2, half3};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float a = h[j] ? A2 : A, b = h[j] ? B2 : B;
+        const float D = *d[j];
+        const float pn = a * sm[j * sp] + b * (a * sm[(4 + j) * sp] + D);  // psi = A psi + B (A prev + D)
+        reinterpret_cast<float*>(p.psi[ax][slot0 + j])[so] = pn;
+        reinterpret_cast<float*>(p.prv[ax][slot0 + j])[so] = D;
+        *d[j] = D + pn;
+    }
+}
+
 // CPML of the four derivatives of one axis for both cells of a pair (in[c]: cell c lies in the slab, at element
 // so[c] of the axis' memory arrays): all sixteen loads first, then the updates, then the stores.  The arrays cannot
 // alias, but the compiler cannot know; batching the pair's loads keeps one memory latency per axis instead of one
@@ -171,12 +192,17 @@ __device__ __forceinline__ void pml4x2(const DevPtrs& p, int ax, int slot0, cons
 // CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
 // velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.  PAIRED: the
 // two cells' memory loads of an axis batched (pml4x2: one memory latency per axis); else cell by cell (pml4: fewer
-// live registers, for kernels at their register limit).  Both give the same bits.
-template <int SLOT0, bool PAIRED>
+// live registers, for kernels at their register limit); XS (cell by cell only): the x-slab memory and the x
+// profiles read from shared memory, xrow being this warp's row of a TMA box that starts at slab index xbase (arrays
+// xplane floats apart) and xprof the pair's entry in the tile's profile boxes (A, B, A2, B2, TXC floats apart).
+// All forms give the same bits.
+template <int SLOT0, bool PAIRED, bool XS = false>
 __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x, int y, int k, bool a0, bool a1,
                                          float2& dx0, float2& dx1, float2& dx2, float2& dx3, const bool hx[4],
                                          float2& dy0, float2& dy1, float2& dy2, float2& dy3, const bool hy[4],
-                                         float2& dz0, float2& dz1, float2& dz2, float2& dz3, const bool hz[4]) {
+                                         float2& dz0, float2& dz1, float2& dz2, float2& dz3, const bool hz[4],
+                                         const float* xrow = nullptr, int xbase = 0, int xplane = 0,
+                                         const float* xprof = nullptr) {
     if constexpr (PAIRED) {
         {
             const int si0 = a0 ? slab_index(x, g.nx, g.L) : -1, si1 = a1 ? slab_index(x + 1, g.nx, g.L) : -1;
@@ -215,8 +241,12 @@ __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x,
             if (si >= 0) {
                 const long long so = ((long long)k * g.ny + y) * g.W + si;
                 float a = comp(dx0, c), b = comp(dx1, c), d = comp(dx2, c), e = comp(dx3, c);
-                pml4(p, 0, SLOT0, so, prof(p.pa[0], xc), prof(p.pb[0], xc), prof(p.pa2[0], xc), prof(p.pb2[0], xc), a, b,
-                     d, e, hx[0], hx[1], hx[2], hx[3]);
+                if constexpr (XS)
+                    pml4_sm(p, 0, SLOT0, so, xrow + (si - xbase), xplane, xprof[c], xprof[TXC + c],
+                            xprof[2 * TXC + c], xprof[3 * TXC + c], a, b, d, e, hx[0], hx[1], hx[2], hx[3]);
+                else
+                    pml4(p, 0, SLOT0, so, prof(p.pa[0], xc), prof(p.pb[0], xc), prof(p.pa2[0], xc), prof(p.pb2[0], xc),
+                         a, b, d, e, hx[0], hx[1], hx[2], hx[3]);
                 setc(dx0, c, a);
                 setc(dx1, c, b);
                 setc(dx2, c, d);
@@ -725,6 +755,20 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
         ok &= encode<S>(&tm->own[q], g, p.f[BEHF_SXX + q], TXC, TY);
         ok &= encode<K>(&tm->own[7 + q], g, p.k[q < 4 ? P1 + q : P1 + q + 1], TXC, TY);
     }
+    // x-slab CPML memory and x profiles, staged by the tensor-memory kernels (FP32 memory)
+    if (g.W > 0 && g.xs_bw > 0 && sizeof(Wt) == 4) {
+        for (int j = 0; j < 4; j++) {
+            ok &= encode_xslab(&vm->xs[j], g, p.psi[0][j], g.xs_bw);
+            ok &= encode_xslab(&vm->xs[4 + j], g, p.prv[0][j], g.xs_bw);
+            ok &= encode_xslab(&tm->xs[j], g, p.psi[0][4 + j], g.xs_bw);
+            ok &= encode_xslab(&tm->xs[4 + j], g, p.prv[0][4 + j], g.xs_bw);
+        }
+        void* const prof[4] = {p.pa[0], p.pb[0], p.pa2[0], p.pb2[0]};
+        for (int j = 0; j < 4; j++) {
+            ok &= encode_prof(&vm->xp[j], g.nx, prof[j]);
+            ok &= encode_prof(&tm->xp[j], g.nx, prof[j]);
+        }
+    }
     return ok;
 }
 
@@ -738,7 +782,7 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     // that, a chunk count that fills the last wave of resident CTAs (MINB per SM) with at least four waves where
     // 16-plane chunks allow it (the autotuner's choice at 128^3-256^3: 0.79 ms per step at 256^3 against 0.89 ms
     // for two waves of 36-plane chunks)
-    const bool ws = g.ws != 0, zq = g.ws == 2;
+    const bool ws = g.ws != 0, zq = g.ws >= 2;
     const int minb = ws ? WDepth<S>::MINB : vel ? Depth<S>::MINB : Depth<S>::MINB_T;
     const int slots = minb * device_sms();
     int zchunk = wave_zchunk(nbx * nby, planes, slots, 16, BEHF_TILED_ZCHUNK, R, BEHF_TILED_MINW);
@@ -753,28 +797,32 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
         });
     };
     cudaError_t e = cudaSuccess;
-    if (zq && vel) {
-        static PerDevice once;
-        const int smem = ZMap<S, R, true>::bytes + 128;
-        if (g.sr && sizeof(S) == 2) {
-            static PerDevice once_sr;
-            if ((e = optin(once_sr, (const void*)k_vel_zq<S, R, true>, smem)) != cudaSuccess) return e;
-            k_vel_zq<S, R, true><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
-        } else {
-            if ((e = optin(once, (const void*)k_vel_zq<S, R, false>, smem)) != cudaSuccess) return e;
-            k_vel_zq<S, R, false><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
-        }
-    } else if (zq) {
-        static PerDevice once;
-        const int smem = ZMap<S, R, false>::bytes + 128;
-        if (g.sr && sizeof(S) == 2) {
-            static PerDevice once_sr;
-            if ((e = optin(once_sr, (const void*)k_str_zq<S, R, true>, smem)) != cudaSuccess) return e;
-            k_str_zq<S, R, true><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
-        } else {
-            if ((e = optin(once, (const void*)k_str_zq<S, R, false>, smem)) != cudaSuccess) return e;
-            k_str_zq<S, R, false><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
-        }
+    if (zq) {
+        // stochastic rounding (16-bit kinds) and the x-slab staging (variant 4, when every x-edge tile's box fits)
+        // select the instantiation; each has its own opt-in flags
+        const bool sr = g.sr && sizeof(S) == 2;
+        const bool xs = g.ws == 3 &&
+                        (vel ? xs_grid_ok<ZMap<S, R, true>>(g, nbx) : xs_grid_ok<ZMap<S, R, false>>(g, nbx));
+        auto go = [&](auto srnd, auto xst) -> cudaError_t {
+            constexpr bool SR_ = decltype(srnd)::value, XS_ = decltype(xst)::value;
+            static PerDevice once_v, once_t;
+            if (vel) {
+                const int smem = ZMap<S, R, true>::bytes + 128;
+                cudaError_t r = optin(once_v, (const void*)k_vel_zq<S, R, SR_, XS_>, smem);
+                if (r != cudaSuccess) return r;
+                k_vel_zq<S, R, SR_, XS_><<<grid, NTH_WS, smem, st>>>(vm, g, p, zchunk);
+            } else {
+                const int smem = ZMap<S, R, false>::bytes + 128;
+                cudaError_t r = optin(once_t, (const void*)k_str_zq<S, R, SR_, XS_>, smem);
+                if (r != cudaSuccess) return r;
+                k_str_zq<S, R, SR_, XS_><<<grid, NTH_WS, smem, st>>>(tm, g, p, zchunk);
+            }
+            return cudaSuccess;
+        };
+        using T_ = std::true_type;
+        using F_ = std::false_type;
+        e = sr ? (xs ? go(T_{}, T_{}) : go(T_{}, F_{})) : (xs ? go(F_{}, T_{}) : go(F_{}, F_{}));
+        if (e != cudaSuccess) return e;
     } else if (ws && vel) {
         static PerDevice once;
         const int smem = WMap<S, R, true>::bytes + 128;

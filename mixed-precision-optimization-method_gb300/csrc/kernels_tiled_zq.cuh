@@ -15,8 +15,11 @@
 //        +c_{R-j+1} (j <= R) / -c_{j-R} (j > R) to D(z-R+j), j = 1..2R.
 // Each CTA allocates 128 TMEM columns (warps w and w + 4 share a 32-lane quarter, 64 columns each: 4 fields x 16);
 // the register limit keeps at most two such CTAs on an SM (256 of the 512 columns), so an allocation never waits.
-// The first 2R planes of a z range arrive in a one-shot warm-up area, whose partial sums are formed in registers.  Every wait is bounded; on any exit path the
-// compute warps meet at a named barrier and warp 0 frees the TMEM.
+// The first 2R planes of a z range arrive in a one-shot warm-up area, whose partial sums are formed in registers;
+// once every compute warp has read it, the tiles at the x edges receive there, with each plane, the CPML memory of
+// their x-slab cells (TMA boxes), so that their slab updates read it from shared memory instead of waiting on
+// global loads.  Every wait is bounded; on any exit path the compute warps meet at a named barrier and warp 0 frees
+// the TMEM.
 #pragma once
 #include <type_traits>
 
@@ -166,21 +169,65 @@ struct ZMap {
     static constexpr uint32_t warm_tx = 4 * 2 * R * G::OWN_B;
 };
 
-// Producer of a ZQ kernel: the warm-up planes kb-R .. kb+R-1 of the z fields on `warm`, then the stages.
-template <class M, int R, class Issue>
+// x-slab CPML memory staged by TMA: the tiles at the x edges bring, with each plane, the memory of their x-slab cells
+// (eight FP32 arrays, boxes of xs_bw x TY) into the warm-up area, which is idle once the warm-up planes are read
+// (one set per stage).  Bytes of one set, and whether this CTA stages (CTA-uniform; xbase from xs_tile_base).
+// After the sets, the tile's four x profiles (TXC values each), brought once with the first plane.
+constexpr int kXsProfBytes = 4 * TXC * 4;
+__host__ __device__ __forceinline__ int xs_set_bytes(const Geom& g) { return 8 * g.xs_bw * TY * 4; }
+template <class M>
+__device__ __forceinline__ bool xs_staged(const Geom& g, int xbase) {
+    return xbase >= 0 && M::NS * xs_set_bytes(g) + kXsProfBytes <= M::bytes - M::warm;
+}
+// Host: whether every tile of the grid that updates x-slab cells can stage them; the launcher then runs the XS
+// instantiation, whose x-slab path reads shared memory only.
+template <class M>
+inline bool xs_grid_ok(const Geom& g, int nbx) {
+    if (g.xs_bw <= 0 || g.W <= 0 || M::NS * xs_set_bytes(g) + kXsProfBytes > M::bytes - M::warm) return false;
+    for (int bx = 0; bx < nbx; bx++) {
+        const int x0 = bx * TXC;
+        const int lo = x0 > g.R ? x0 : g.R, hi = x0 + TXC < g.nx - g.R ? x0 + TXC : g.nx - g.R;
+        if (lo >= hi) continue;
+        if ((lo < g.L || hi > g.nx - 1 - g.L) && xs_tile_base(g, x0) < 0) return false;
+    }
+    return true;
+}
+
+// Producer of a ZQ kernel: the warm-up planes kb-R .. kb+R-1 of the z fields on `warm`, then the stages.  With
+// xs: each stage's x-slab boxes (issue_x) and, with the first plane, the x profiles (issue_p), counted in the
+// stages' expected bytes by `issue`; those of the first stages only after every compute warp has read the warm-up
+// area (`wfree`).
+template <class M, int R, class Issue, class IssueX, class IssueP>
 __device__ __forceinline__ void zq_produce(unsigned char* smem, uint64_t* full, uint64_t* empty, uint64_t* warm,
-                                           const CUtensorMap* zlead, int x0, int y0, int kb, int ke, int* err,
-                                           Issue&& issue) {
+                                           uint64_t* wfree, const CUtensorMap* zlead, int x0, int y0, int kb, int ke,
+                                           int* err, bool xs, Issue&& issue, IssueX&& issue_x, IssueP&& issue_p) {
     mbar_expect_tx(warm, M::warm_tx);
     for (int w = 0; w < 2 * R; w++)
 #pragma unroll
         for (int f = 0; f < 4; f++) tma3(smem + M::warm + (f * 2 * R + w) * M::OW, &zlead[f], warm, x0, y0, kb - R + w);
-    ws_produce<M::NS>(full, empty, kb, ke, err, [&](int st, int k, bool) { issue(st, k); });
+    const int nfirst = ke - kb < M::NS ? ke - kb : M::NS;
+    bool xok = xs;
+    ws_produce<M::NS>(full, empty, kb, ke, err, [&](int st, int k, bool) {
+        issue(st, k);
+        if (!xok) return;
+        const int it = k - kb;
+        if (it >= M::NS) {
+            issue_x(st, k);
+        } else if (it == nfirst - 1) {
+            if (!mbar_wait(wfree, 0)) {  // the compute warps never finished the warm-up: their waits run out too
+                xok = false;
+                atomicExch(err, 1);
+                return;
+            }
+            issue_p();
+            for (int i = 0; i < nfirst; i++) issue_x(i % M::NS, kb + i);
+        }
+    });
     mbar_wait(warm, 0);
 }
 
 // ----------------------------------------------------------------------------------------- velocity
-template <class S, int R, bool SRND>
+template <class S, int R, bool SRND, bool XS>
 __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     k_vel_zq(const __grid_constant__ VMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
     typedef Pair<S> PS;
@@ -191,7 +238,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     typedef ZMap<S, R, true> M;
     constexpr int NS = M::NS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS], bwarm;
+    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS], bwarm, bwfree;
     __shared__ uint32_t tbase;
     unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
@@ -206,6 +253,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             mbar_init(&bempty[s], NWARP);
         }
         mbar_init(&bwarm, 1);
+        mbar_init(&bwfree, NWARP);
         fence_init();
     }
     if (ty == 0) tm_alloc(&tbase);
@@ -215,10 +263,13 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 
     if (ty == NWARP) {  // producer warp
         if (tx == 0) {
+            const int xbase = xs_tile_base(g, x0);
+            const bool xs = XS && xs_staged<M>(g, xbase);
+            const int xsb = xs_set_bytes(g);
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
-                mbar_expect_tx(br, M::stage_tx);
+                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xsb + (k == kb ? kXsProfBytes : 0)) : 0u));
                 tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0, k);      // txx  (x halo)
                 tma3(b + M::halo(1), &maps.halo[1], br, x0, y0 - R, k);          // tyy  (y halo)
                 tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // txy  (x, y halo)
@@ -234,7 +285,18 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 #pragma unroll
                 for (int f = 0; f < 4; f++) tma3(b + M::zl + f * M::OW, &maps.zlead[f], br, x0, y0, k + R);
             };
-            zq_produce<M, R>(smem, bfull, bempty, &bwarm, maps.zlead, x0, y0, kb, ke, g.err, issue);
+            auto issue_x = [&](int st, int k) {
+                unsigned char* xb = smem + M::warm + st * xsb;
+#pragma unroll
+                for (int j = 0; j < 8; j++) tma3(xb + j * (xsb / 8), &maps.xs[j], &bfull[st], xbase, y0, k);
+            };
+            auto issue_p = [&]() {  // on the first plane's stage (stage 0)
+                unsigned char* pb = smem + M::warm + NS * xsb;
+#pragma unroll
+                for (int j = 0; j < 4; j++) tma1(pb + j * (kXsProfBytes / 4), &maps.xp[j], &bfull[0], x0);
+            };
+            zq_produce<M, R>(smem, bfull, bempty, &bwarm, &bwfree, maps.zlead, x0, y0, kb, ke, g.err, xs, issue,
+                             issue_x, issue_p);
         }
         return;
     }
@@ -278,6 +340,8 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         warm(3, v);
         zq_warm<R, FWD3>(ta + 48, v);
     }
+    __syncwarp();
+    if (tx == 0) mbar_arrive(&bwfree);  // the warm-up area is read: the producer may stage x-slab memory there
 
 #pragma unroll kZqUnroll
     for (int k = kb, it = 0; k < ke && !failed; k++, it++) {
@@ -324,8 +388,15 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         if (live) {
             const long long go = (long long)k * g.plane + col;
             if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
+                // XS: the x-slab memory staged in the warm-up area (formed here: nothing extra stays live in the loop)
+                const int xbase = XS ? xs_tile_base(g, x0) : 0;
+                const float* xrow =
+                    XS ? reinterpret_cast<const float*>(smem + M::warm + st * xs_set_bytes(g)) + ty * g.xs_bw : nullptr;
+                const float* xprof =
+                    XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {true, true, false, false};
-                pml_pair<0, false>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf);
+                pml_pair<0, false, XS>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf,
+                                       xrow, xbase, g.xs_bw * TY, xprof);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
@@ -374,7 +445,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 }
 
 // ----------------------------------------------------------------------------------------- stress
-template <class S, int R, bool SRND>
+template <class S, int R, bool SRND, bool XS>
 __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     k_str_zq(const __grid_constant__ TMaps maps, const Geom g, const DevPtrs p, const int zchunk) {
     typedef Pair<S> PS;
@@ -385,7 +456,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     typedef ZMap<S, R, false> M;
     constexpr int NS = M::NS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS], bwarm;
+    __shared__ __align__(8) uint64_t bfull[NS], bempty[NS], bwarm, bwfree;
     __shared__ uint32_t tbase;
     unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
@@ -400,6 +471,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             mbar_init(&bempty[s], NWARP);
         }
         mbar_init(&bwarm, 1);
+        mbar_init(&bwfree, NWARP);
         fence_init();
     }
     if (ty == 0) tm_alloc(&tbase);
@@ -409,10 +481,13 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 
     if (ty == NWARP) {  // producer warp
         if (tx == 0) {
+            const int xbase = xs_tile_base(g, x0);
+            const bool xs = XS && xs_staged<M>(g, xbase);
+            const int xsb = xs_set_bytes(g);
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
-                mbar_expect_tx(br, M::stage_tx);
+                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xsb + (k == kb ? kXsProfBytes : 0)) : 0u));
                 tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0 - R, k);  // vx (x, y halo)
                 tma3(b + M::halo(1), &maps.halo[1], br, x0 - G::HX, y0 - R, k);  // vy
                 tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
@@ -425,7 +500,18 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
 #pragma unroll
                 for (int f = 0; f < 4; f++) tma3(b + M::zl + f * M::OW, &maps.zlead[f], br, x0, y0, k + R);
             };
-            zq_produce<M, R>(smem, bfull, bempty, &bwarm, maps.zlead, x0, y0, kb, ke, g.err, issue);
+            auto issue_x = [&](int st, int k) {
+                unsigned char* xb = smem + M::warm + st * xsb;
+#pragma unroll
+                for (int j = 0; j < 8; j++) tma3(xb + j * (xsb / 8), &maps.xs[j], &bfull[st], xbase, y0, k);
+            };
+            auto issue_p = [&]() {  // on the first plane's stage (stage 0)
+                unsigned char* pb = smem + M::warm + NS * xsb;
+#pragma unroll
+                for (int j = 0; j < 4; j++) tma1(pb + j * (kXsProfBytes / 4), &maps.xp[j], &bfull[0], x0);
+            };
+            zq_produce<M, R>(smem, bfull, bempty, &bwarm, &bwfree, maps.zlead, x0, y0, kb, ke, g.err, xs, issue,
+                             issue_x, issue_p);
         }
         return;
     }
@@ -467,6 +553,8 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         warm(3, v);
         zq_warm<R, FWD3>(ta + 48, v);
     }
+    __syncwarp();
+    if (tx == 0) mbar_arrive(&bwfree);  // the warm-up area is read: the producer may stage x-slab memory there
 
 #pragma unroll kZqUnroll
     for (int k = kb, it = 0; k < ke && !failed; k++, it++) {
@@ -512,8 +600,14 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
         if (live) {
             const long long go = (long long)k * g.plane + col;
             if (xy_slab || (g.W > 0 && slab_index(k, g.nz, g.L) >= 0)) {
+                const int xbase = XS ? xs_tile_base(g, x0) : 0;
+                const float* xrow =
+                    XS ? reinterpret_cast<const float*>(smem + M::warm + st * xs_set_bytes(g)) + ty * g.xs_bw : nullptr;
+                const float* xprof =
+                    XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {false, false, true, true};
-                pml_pair<4, false>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz, uyz, hf);
+                pml_pair<4, false, XS>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz,
+                                       uyz, hf, xrow, xbase, g.xs_bw * TY, xprof);
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);
