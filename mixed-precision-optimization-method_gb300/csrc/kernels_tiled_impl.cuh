@@ -99,10 +99,12 @@ __device__ __forceinline__ void pml4(const DevPtrs& p, int ax, int slot0, long l
         pv[j] = reinterpret_cast<float*>(p.prv[ax][slot0 + j]) + so;
     }
     float s[4], v[4];
+    // read-only-path loads: a slab element is read once, before the same thread writes it, in a launch, so the
+    // non-coherent path is exact, and it lets the compiler start the next cell's loads before this cell's stores
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        s[j] = *ps[j];
-        v[j] = *pv[j];
+        s[j] = __ldg(ps[j]);
+        v[j] = __ldg(pv[j]);
     }
     float* d[4] = {&d0, &d1, &d2, &d3};
     const bool h[4] = {half0, half1, half2, half3};
