@@ -28,9 +28,8 @@ thread_local std::string g_err;
 // FP16 30.5 / 33.7 / 35.2, BF16 28.7 / 32.1 / 34.0, FP32 20.8 / 21.7 / 21.2 Gpt/s for classic / warp-specialised /
 // tensor-memory z).
 // Automatic tiled-kernel variant (Geom::ws = BEHF_OPT_TILED_VARIANT - 1), the fastest measured at 1024^3: the tensor-
-// memory kernels with the x-slab staging for FP16, without it for BF16 (its stress kernel spills more with it),
-// the warp-specialised kernels for FP32.
-int auto_variant(int precision) { return precision == BEHF_FP16 ? 3 : precision == BEHF_BF16 ? 2 : 1; }
+// memory kernels with the x-slab staging for FP16 and BF16, the warp-specialised kernels for FP32.
+int auto_variant(int precision) { return precision == BEHF_FP16 || precision == BEHF_BF16 ? 3 : 1; }
 
 behf_status fail(behf_status code, const char* fmt, ...) {
     char buf[512];
@@ -513,6 +512,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     // the tensor-memory kernels' TMA box of x-slab memory: an edge tile's slab cells (at most L + 1, at most a tile
     // row of 64) plus up to 3 cells of alignment
     g.xs_bw = L > 0 ? std::min(64, (std::min(L + 1, 64) + 3 + 3) / 4 * 4) : 0;
+    g.slab_pf = L > 0 && gr->nx % 4 == 0 ? 1 : 0;
     g.px = ((long long)gr->nx + 15) / 16 * 16;
     g.plane = g.px * gr->ny;
     g.bug = 0;

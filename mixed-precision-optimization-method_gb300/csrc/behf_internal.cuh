@@ -113,6 +113,7 @@ struct Geom {
     int nx, ny, nz;
     int R, L, W;           // stencil half-width, CPML width, slab pitch (2L+1 rounded up to 4; 0 without CPML)
     int xs_bw;             // tensor-memory kernels: width of the TMA box of x-slab CPML memory (0: none)
+    int slab_pf;           // tensor-memory kernels: 1 when the y/z-slab tensor maps exist (L2 prefetch of slab memory)
     long long px, plane;   // row pitch and plane stride in elements
     int bug;               // reference vz/VW3y compatibility
     int* err;              // device error word: set to 1 by a kernel whose bounded wait timed out

@@ -115,6 +115,7 @@ struct VMaps {
     CUtensorMap own[18];
     CUtensorMap xs[8];    // x-slab CPML memory of slots 0..3 (psi 0..3, then prev 0..3): boxes xs_bw x TY x 1
     CUtensorMap xp[4];    // x damping profiles A, B, A2, B2: 1-D boxes of TXC
+    CUtensorMap ys[8], zs[8];  // y- and z-slab CPML memory of slots 0..3 (L2 prefetch): boxes TXC x TY x 1
 };
 struct TMaps {
     CUtensorMap halo[5];  // vx vy vz (XY) qx (X) qy (Y)
@@ -122,6 +123,7 @@ struct TMaps {
     CUtensorMap own[14];  // sxx syy szz sxy sxz syz p, then P1 P2 S1 S2 Sxy Sxz Syz
     CUtensorMap xs[8];    // x-slab CPML memory of slots 4..7 (psi, then prev)
     CUtensorMap xp[4];    // x damping profiles A, B, A2, B2
+    CUtensorMap ys[8], zs[8];  // y- and z-slab CPML memory of slots 4..7 (L2 prefetch)
 };
 
 // ------------------------------------------------------------------------------------- PTX helpers
@@ -160,6 +162,13 @@ __device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, uint64_t
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
         : "memory");
+}
+// L2 prefetch of one box (no shared memory, no barrier; out-of-range parts are skipped).
+__device__ __forceinline__ void tma3_prefetch(const CUtensorMap* map, int x, int y, int z) {
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(x), "r"(y), "r"(z)
+                 : "memory");
 }
 __device__ __forceinline__ void tma1(void* dst, const CUtensorMap* map, uint64_t* bar, int x) {
     asm volatile(
@@ -299,6 +308,20 @@ inline bool encode_xslab(CUtensorMap* m, const Geom& g, void* base, int bw) {
     const cuuint64_t dims[3] = {(cuuint64_t)g.W, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
     const cuuint64_t strides[2] = {(cuuint64_t)g.W * 4, (cuuint64_t)g.W * g.ny * 4};
     const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)TY, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// 3-D map over an FP32 array of dims (d0, d1, d2) (innermost first; d0 a multiple of 4), box TXC x TY x 1: the y-
+// ([nz][W][nx]: nx, W, nz) and z-slab ([W][ny][nx]: nx, ny, W) CPML memory, for L2 prefetches of a tile's rows.
+inline bool encode_slab(CUtensorMap* m, void* base, int d0, int d1, int d2) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    const cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)d0 * d1 * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)TXC, (cuuint32_t)TY, 1};
     const cuuint32_t es[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

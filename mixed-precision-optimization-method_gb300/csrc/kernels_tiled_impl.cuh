@@ -190,15 +190,14 @@ __device__ __forceinline__ void pml4x2(const DevPtrs& p, int ax, int slot0, cons
         }
     }
 }
-
 // CPML for the pair: x per cell, y per row (warp-uniform), z per plane (CTA-uniform).  Slots 0..3 of the
 // velocity kernel / 4..7 of the stress kernel; `half` flags mark forward (half-shifted) derivatives.  PAIRED: the
-// two cells' memory loads of an axis batched (pml4x2: one memory latency per axis); else cell by cell (pml4: fewer
-// live registers, for kernels at their register limit); XS (cell by cell only): the x-slab memory and the x
-// profiles read from shared memory, xrow being this warp's row of a TMA box that starts at slab index xbase (arrays
-// xplane floats apart) and xprof the pair's entry in the tile's profile boxes (A, B, A2, B2, TXC floats apart).
-// All forms give the same bits.
-template <int SLOT0, bool PAIRED, bool XS = false>
+// x slab's two cells batched (pml4x2: one memory latency instead of two); else cell by cell (pml4: fewer live
+// registers), or XS: the x-slab memory and the x profiles read from shared memory, xrow being this warp's row of a
+// TMA box that starts at slab index xbase (arrays xplane floats apart) and xprof the pair's entry in the tile's
+// profile boxes (A, B, A2, B2, TXC floats apart).  PAIRYZ: the y and z slabs' two cells batched likewise.  All
+// forms give the same bits.
+template <int SLOT0, bool PAIRED, bool XS = false, bool PAIRYZ = PAIRED>
 __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x, int y, int k, bool a0, bool a1,
                                          float2& dx0, float2& dx1, float2& dx2, float2& dx3, const bool hx[4],
                                          float2& dy0, float2& dy1, float2& dy2, float2& dy3, const bool hy[4],
@@ -206,34 +205,16 @@ __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x,
                                          const float* xrow = nullptr, int xbase = 0, int xplane = 0,
                                          const float* xprof = nullptr) {
     if constexpr (PAIRED) {
-        {
-            const int si0 = a0 ? slab_index(x, g.nx, g.L) : -1, si1 = a1 ? slab_index(x + 1, g.nx, g.L) : -1;
-            if (si0 >= 0 || si1 >= 0) {
-                const bool in[2] = {si0 >= 0, si1 >= 0};
-                const long long row = ((long long)k * g.ny + y) * g.W;
-                const long long so[2] = {row + si0, row + si1};
-                auto pr = [&](void* const* t) {
-                    return f2(in[0] ? prof(t[0], x) : 0.f, in[1] ? prof(t[0], x + 1) : 0.f);
-                };
-                pml4x2(p, 0, SLOT0, so, in, pr(p.pa), pr(p.pb), pr(p.pa2), pr(p.pb2), dx0, dx1, dx2, dx3, hx[0], hx[1],
-                       hx[2], hx[3]);
-            }
-        }
-        const int sj = slab_index(y, g.ny, g.L);
-        if (sj >= 0) {
-            const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
-            const bool in[2] = {a0, a1};
-            const long long so[2] = {((long long)k * g.W + sj) * g.nx + x, ((long long)k * g.W + sj) * g.nx + x + 1};
-            pml4x2(p, 1, SLOT0, so, in, f2(A, A), f2(B, B), f2(A2, A2), f2(B2, B2), dy0, dy1, dy2, dy3, hy[0], hy[1],
-                   hy[2], hy[3]);
-        }
-        const int sk = slab_index(k, g.nz, g.L);
-        if (sk >= 0) {
-            const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
-            const bool in[2] = {a0, a1};
-            const long long so[2] = {((long long)sk * g.ny + y) * g.nx + x, ((long long)sk * g.ny + y) * g.nx + x + 1};
-            pml4x2(p, 2, SLOT0, so, in, f2(A, A), f2(B, B), f2(A2, A2), f2(B2, B2), dz0, dz1, dz2, dz3, hz[0], hz[1],
-                   hz[2], hz[3]);
+        const int si0 = a0 ? slab_index(x, g.nx, g.L) : -1, si1 = a1 ? slab_index(x + 1, g.nx, g.L) : -1;
+        if (si0 >= 0 || si1 >= 0) {
+            const bool in[2] = {si0 >= 0, si1 >= 0};
+            const long long row = ((long long)k * g.ny + y) * g.W;
+            const long long so[2] = {row + si0, row + si1};
+            auto pr = [&](void* const* t) {
+                return f2(in[0] ? prof(t[0], x) : 0.f, in[1] ? prof(t[0], x + 1) : 0.f);
+            };
+            pml4x2(p, 0, SLOT0, so, in, pr(p.pa), pr(p.pb), pr(p.pa2), pr(p.pb2), dx0, dx1, dx2, dx3, hx[0], hx[1],
+                   hx[2], hx[3]);
         }
     } else {
 #pragma unroll
@@ -255,37 +236,34 @@ __device__ __forceinline__ void pml_pair(const Geom& g, const DevPtrs& p, int x,
                 setc(dx3, c, e);
             }
         }
-        const int sj = slab_index(y, g.ny, g.L);
-        if (sj >= 0) {
-            const float A = prof(p.pa[1], y), B = prof(p.pb[1], y), A2 = prof(p.pa2[1], y), B2 = prof(p.pb2[1], y);
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (!(c ? a1 : a0)) continue;
-                const long long so = ((long long)k * g.W + sj) * g.nx + x + c;
-                float a = comp(dy0, c), b = comp(dy1, c), d = comp(dy2, c), e = comp(dy3, c);
-                pml4(p, 1, SLOT0, so, A, B, A2, B2, a, b, d, e, hy[0], hy[1], hy[2], hy[3]);
-                setc(dy0, c, a);
-                setc(dy1, c, b);
-                setc(dy2, c, d);
-                setc(dy3, c, e);
-            }
-        }
-        const int sk = slab_index(k, g.nz, g.L);
-        if (sk >= 0) {
-            const float A = prof(p.pa[2], k), B = prof(p.pb[2], k), A2 = prof(p.pa2[2], k), B2 = prof(p.pb2[2], k);
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (!(c ? a1 : a0)) continue;
-                const long long so = ((long long)sk * g.ny + y) * g.nx + x + c;
-                float a = comp(dz0, c), b = comp(dz1, c), d = comp(dz2, c), e = comp(dz3, c);
-                pml4(p, 2, SLOT0, so, A, B, A2, B2, a, b, d, e, hz[0], hz[1], hz[2], hz[3]);
-                setc(dz0, c, a);
-                setc(dz1, c, b);
-                setc(dz2, c, d);
-                setc(dz3, c, e);
-            }
-        }
     }
+    // y (slab index sj, memory [nz][W][nx]) and z (sk, [W][ny][nx]): both cells share the profiles
+    auto yz = [&](int ax, long long base, float2& e0, float2& e1, float2& e2, float2& e3, const bool hh[4]) {
+        const int pos = ax == 1 ? y : k;
+        const float A = prof(p.pa[ax], pos), B = prof(p.pb[ax], pos), A2 = prof(p.pa2[ax], pos),
+                    B2 = prof(p.pb2[ax], pos);
+        if constexpr (PAIRYZ) {
+            const bool in[2] = {a0, a1};
+            const long long so[2] = {base, base + 1};
+            pml4x2(p, ax, SLOT0, so, in, f2(A, A), f2(B, B), f2(A2, A2), f2(B2, B2), e0, e1, e2, e3, hh[0], hh[1],
+                   hh[2], hh[3]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                if (!(c ? a1 : a0)) continue;
+                float a = comp(e0, c), b = comp(e1, c), d = comp(e2, c), e = comp(e3, c);
+                pml4(p, ax, SLOT0, base + c, A, B, A2, B2, a, b, d, e, hh[0], hh[1], hh[2], hh[3]);
+                setc(e0, c, a);
+                setc(e1, c, b);
+                setc(e2, c, d);
+                setc(e3, c, e);
+            }
+        }
+    };
+    const int sj = slab_index(y, g.ny, g.L);
+    if (sj >= 0) yz(1, ((long long)k * g.W + sj) * g.nx + x, dy0, dy1, dy2, dy3, hy);
+    const int sk = slab_index(k, g.nz, g.L);
+    if (sk >= 0) yz(2, ((long long)sk * g.ny + y) * g.nx + x, dz0, dz1, dz2, dz3, hz);
 }
 
 // Store a pair, or the one active cell of it.
@@ -771,6 +749,18 @@ bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
             ok &= encode_prof(&tm->xp[j], g.nx, prof[j]);
         }
     }
+    // y- and z-slab CPML memory (L2 prefetch boxes; their rows are 16-byte multiples only when nx is a multiple of 4)
+    if (g.slab_pf)
+        for (int j = 0; j < 8; j++) {
+            void* const vy = j < 4 ? p.psi[1][j] : p.prv[1][j - 4];
+            void* const vz = j < 4 ? p.psi[2][j] : p.prv[2][j - 4];
+            void* const ty = j < 4 ? p.psi[1][4 + j] : p.prv[1][j];
+            void* const tz = j < 4 ? p.psi[2][4 + j] : p.prv[2][j];
+            ok &= encode_slab(&vm->ys[j], vy, g.nx, g.W, g.nz);
+            ok &= encode_slab(&vm->zs[j], vz, g.nx, g.ny, g.W);
+            ok &= encode_slab(&tm->ys[j], ty, g.nx, g.W, g.nz);
+            ok &= encode_slab(&tm->zs[j], tz, g.nx, g.ny, g.W);
+        }
     return ok;
 }
 

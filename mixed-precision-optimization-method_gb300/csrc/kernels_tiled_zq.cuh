@@ -29,11 +29,17 @@ namespace tiled {
 #ifndef BEHF_ZQ_NS
 #define BEHF_ZQ_NS 2
 #endif
-// Plane loop unrolled by the stage count, so that each copy's stage (and its shared-memory offsets) is fixed.
+// Plane-loop unrolling.  Unrolled by the stage count, each copy's stage (and its shared-memory offsets) is fixed, but
+// the loop's code doubles and competes for the instruction cache (instruction-fetch stalls were the second stall):
+// not unrolled, 1024^3 FP16 runs at 39.2 Gpt/s against 37.9 unrolled by two (BF16 36.3 against 35.4).
 #ifndef BEHF_ZQ_UNROLL
-#define BEHF_ZQ_UNROLL 2
+#define BEHF_ZQ_UNROLL 1
 #endif
 constexpr int kZqUnroll = BEHF_ZQ_UNROLL;
+// y- and z-slab CPML memory of a cell pair loaded in one batch (one memory latency instead of two)
+#ifndef BEHF_ZQ_PAIRYZ
+#define BEHF_ZQ_PAIRYZ true
+#endif
 constexpr uint32_t kZqCols = 128;  // TMEM columns per CTA
 
 // Store a cell pair; FULL: both cells are known to be updated (no per-cell guard).
@@ -179,6 +185,32 @@ template <class M>
 __device__ __forceinline__ bool xs_staged(const Geom& g, int xbase) {
     return xbase >= 0 && M::NS * xs_set_bytes(g) + kXsProfBytes <= M::bytes - M::warm;
 }
+// L2 prefetch, by the producer, of the y- and z-slab CPML memory (and the x-slab memory where it is not staged)
+// that plane k's slab cells will load: a few tensor prefetches per plane instead of the compute warps' global loads
+// missing L2.  ybox: the first slab row index of the tile's y-slab box, or -1 (no y-slab rows); xbox likewise for
+// an x-slab box read by the compute threads.
+template <class Maps>
+__device__ __forceinline__ void slab_prefetch(const Geom& g, const Maps& maps, int x0, int y0, int k, int ybox,
+                                              int xbox) {
+    if (!g.slab_pf) return;
+    const int sk = slab_index(k, g.nz, g.L);
+    if (sk >= 0)
+        for (int j = 0; j < 8; j++) tma3_prefetch(&maps.zs[j], x0, y0, sk);
+    if (ybox >= 0)
+        for (int j = 0; j < 8; j++) tma3_prefetch(&maps.ys[j], x0, ybox, k);
+    if (xbox >= 0)
+        for (int j = 0; j < 8; j++) tma3_prefetch(&maps.xs[j], xbox, y0, k);
+}
+// The tile's y-slab box start (the slab index of its first updated slab row), or -1.
+__device__ __forceinline__ int ys_tile_box(const Geom& g, int y0) {
+    if (g.W <= 0) return -1;
+    for (int r = 0; r < TY; r++) {
+        const int y = y0 + r;
+        if (y >= g.R && y < g.ny - g.R && slab_index(y, g.ny, g.L) >= 0) return slab_index(y, g.ny, g.L);
+    }
+    return -1;
+}
+
 // Host: whether every tile of the grid that updates x-slab cells can stage them; the launcher then runs the XS
 // instantiation, whose x-slab path reads shared memory only.
 template <class M>
@@ -266,6 +298,11 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             const int xbase = xs_tile_base(g, x0);
             const bool xs = XS && xs_staged<M>(g, xbase);
             const int xsb = xs_set_bytes(g);
+            // L2 prefetch of the slab memory in the instantiation without x staging (measured: BF16 +2.0 %; with the
+            // staging it cost FP16 1.4 %, so that instantiation has none)
+            const int ybox = XS ? -1 : ys_tile_box(g, y0), xbox = XS ? -1 : xbase;
+            if (!XS)
+                for (int k = kb; k < ke && k < kb + NS; k++) slab_prefetch(g, maps, x0, y0, k, ybox, xbox);
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
@@ -284,6 +321,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 for (int j = 0; j < 9; j++) tma3(b + M::own_k + j * M::OK, &maps.own[9 + j], br, x0, y0, k);
 #pragma unroll
                 for (int f = 0; f < 4; f++) tma3(b + M::zl + f * M::OW, &maps.zlead[f], br, x0, y0, k + R);
+                if (!XS && k + NS < ke) slab_prefetch(g, maps, x0, y0, k + NS, ybox, xbox);  // the plane NS ahead
             };
             auto issue_x = [&](int st, int k) {
                 unsigned char* xb = smem + M::warm + st * xsb;
@@ -395,7 +433,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 const float* xprof =
                     XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {true, true, false, false};
-                pml_pair<0, false, XS>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf,
+                pml_pair<0, false, XS, BEHF_ZQ_PAIRYZ>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf,
                                        xrow, xbase, g.xs_bw * TY, xprof);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
@@ -484,6 +522,11 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             const int xbase = xs_tile_base(g, x0);
             const bool xs = XS && xs_staged<M>(g, xbase);
             const int xsb = xs_set_bytes(g);
+            // L2 prefetch of the slab memory in the instantiation without x staging (measured: BF16 +2.0 %; with the
+            // staging it cost FP16 1.4 %, so that instantiation has none)
+            const int ybox = XS ? -1 : ys_tile_box(g, y0), xbox = XS ? -1 : xbase;
+            if (!XS)
+                for (int k = kb; k < ke && k < kb + NS; k++) slab_prefetch(g, maps, x0, y0, k, ybox, xbox);
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
@@ -499,6 +542,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 for (int j = 0; j < 7; j++) tma3(b + M::own_k + j * M::OK, &maps.own[7 + j], br, x0, y0, k);
 #pragma unroll
                 for (int f = 0; f < 4; f++) tma3(b + M::zl + f * M::OW, &maps.zlead[f], br, x0, y0, k + R);
+                if (!XS && k + NS < ke) slab_prefetch(g, maps, x0, y0, k + NS, ybox, xbox);  // the plane NS ahead
             };
             auto issue_x = [&](int st, int k) {
                 unsigned char* xb = smem + M::warm + st * xsb;
@@ -606,7 +650,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                 const float* xprof =
                     XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {false, false, true, true};
-                pml_pair<4, false, XS>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz,
+                pml_pair<4, false, XS, BEHF_ZQ_PAIRYZ>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz,
                                        uyz, hf, xrow, xbase, g.xs_bw * TY, xprof);
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
