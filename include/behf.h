@@ -111,7 +111,7 @@ enum {
     BEHF_OPT_CHECKPOINT_OUTER = 9, /* gradient: outer checkpoint spacing of the two-level scheme, rounded up to a
                                     multiple of BEHF_OPT_CHECKPOINT (0 = automatic: one level when it fits the
                                     device memory, else two levels with the inner spacing halved until they fit) */
-    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic (4), 1 = classic (own-cell data by direct loads of the
+    BEHF_OPT_TILED_VARIANT = 10, /* tiled kernels: 0 = automatic (4 for FP16 / BF16, 2 for FP32), 1 = classic (own-cell data by direct loads of the
                                     compute threads), 2 = warp-specialised (a producer warp brings every input,
                                     own-cell data included, through TMA), 3 = warp-specialised with the z derivatives
                                     accumulated plane by plane in tensor memory (TMEM), 4 = 3 with the CPML memory
