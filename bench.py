@@ -43,7 +43,7 @@ UNIT = "Gpt/s"
 # tensor-memory kernels (variant 4 with the x slabs staged, the FP16 default; variant 3 without), from ncu captures
 # of a 384^3 grid with a 7-cell CPML (the same slab fraction of the grid as 20 cells at 1024^3; one kernel and two
 # launches per capture, 5 GB on the device); the bench multiplies by the cells of its own grid.
-NCU_BYTES_PER_CELL = {("f16", "tmem_xs", "velocity"): 83.92, ("f16", "tmem_xs", "stress"): 67.02,
+NCU_BYTES_PER_CELL = {("f16", "tmem_xs", "velocity"): 81.73, ("f16", "tmem_xs", "stress"): 65.30,
                       ("f16", "tmem", "velocity"): 84.57, ("f16", "tmem", "stress"): 68.47}
 NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per cell of one 384^3 launch with a 7-cell CPML "
               "(profiles/traffic_k_vel_zq_k_str_zq_random384_f16.md), x cells")
