@@ -28,9 +28,10 @@ thread_local std::string g_err;
 // FP16 30.5 / 33.7 / 35.2, BF16 28.7 / 32.1 / 34.0, FP32 20.8 / 21.7 / 21.2 Gpt/s for classic / warp-specialised /
 // tensor-memory z).
 // Automatic tiled-kernel variant (Geom::ws = BEHF_OPT_TILED_VARIANT - 1): the tensor-memory kernels with the x-slab
-// staging for FP16 and BF16, the fastest at 1024^3; the warp-specialised kernels for FP32, whose z derivatives sum
-// each tap pair's difference (the tensor-memory kernels add the taps one by one: 5 % faster in FP32, but their
-// rounding moved a 400-step FP32 gradient to 2.6e-4 of the FP64 adjoint, beyond the 1e-4 bar).
+// staging for FP16 and BF16, the fastest at 1024^3; the warp-specialised kernels for FP32, whose z derivatives
+// alternate the taps of each pair (the tensor-memory kernels add them in plane order, one sign after the other:
+// 5 % faster in FP32, but their rounding moved a 400-step FP32 gradient to 2.6e-4 of the FP64 adjoint, beyond the
+// 1e-4 bar).
 int auto_variant(int precision) { return precision == BEHF_FP16 || precision == BEHF_BF16 ? 3 : 1; }
 
 behf_status fail(behf_status code, const char* fmt, ...) {
