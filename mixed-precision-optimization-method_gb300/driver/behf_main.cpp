@@ -2,7 +2,8 @@
 // of callCUDAKernel (main.cpp:59-1760, kernel.cu:1728-2571) on one GPU.
 //
 //   behf_run [--preset borehole|small64|layered256|random1024] [--scale S] [--nt N] [--precision f16|bf16|f32|f64]
-//            [--radius R] [--kernel auto|plain|tiled] [--snap 1000,2000,3000] [--snap-field sxx]
+//            [--radius R] [--kernel auto|plain|tiled] [--variant auto|classic|ws|tmem|tmem_xs]
+//            [--snap 1000,2000,3000] [--snap-field sxx]
 //            [--out DIR] [--format text|binary|both] [--chunk N] [--ref-bug-compat 0|1] [--quiet] [--setup-only]
 //
 // It sets up the problem (grid, medium, CPML, Ricker source, receivers), runs the time loop through the C ABI
@@ -53,6 +54,7 @@ struct Options {
     std::string precision;
     int radius = 0;
     std::string kernel = "auto";
+    int variant = 0;  // BEHF_OPT_TILED_VARIANT (0 automatic)
     std::vector<int> snaps;
     bool snaps_set = false;
     int snap_field = BEHF_SXX;
@@ -82,6 +84,7 @@ void usage(FILE* f) {
     std::fprintf(f,
                  "usage: behf_run [--preset borehole|small64|layered256|random1024] [--scale S] [--nt N]\n"
                  "                [--precision f16|bf16|f32|f64] [--radius R] [--kernel auto|plain|tiled]\n"
+                 "                [--variant auto|classic|ws|tmem|tmem_xs]\n"
                  "                [--snap it,it,...] [--snap-field NAME] [--out DIR] [--format text|binary|both]\n"
                  "                [--chunk N] [--ref-bug-compat 0|1] [--quiet] [--setup-only]\n");
 }
@@ -133,6 +136,13 @@ bool parse(int argc, char** argv, Options& o) {
             o.radius = std::atoi(v);
         } else if (a == "--kernel") {
             o.kernel = v;
+        } else if (a == "--variant") {
+            const std::string t = v;
+            const char* const names[5] = {"auto", "classic", "ws", "tmem", "tmem_xs"};
+            o.variant = -1;
+            for (int q = 0; q < 5; q++)
+                if (t == names[q]) o.variant = q;
+            if (o.variant < 0) return false;
         } else if (a == "--snap") {
             o.snaps.clear();
             o.snaps_set = true;
@@ -451,6 +461,8 @@ int main(int argc, char** argv) {
     if (p.bug && (st = behf_set_option(ctx.c, BEHF_OPT_REF_BUG_COMPAT, 1))) return lib_fail("set_option", st);
     const int kern = o.kernel == "plain" ? BEHF_KERNEL_PLAIN : o.kernel == "tiled" ? BEHF_KERNEL_TILED : BEHF_KERNEL_AUTO;
     if ((st = behf_set_option(ctx.c, BEHF_OPT_KERNEL, kern))) return lib_fail("set_option(kernel)", st);
+    if (o.variant > 0 && (st = behf_set_option(ctx.c, BEHF_OPT_TILED_VARIANT, o.variant)))
+        return lib_fail("set_option(variant)", st);
     if (o.chunk >= 0 && (st = behf_set_option(ctx.c, BEHF_OPT_GRAPH_CHUNK, o.chunk))) return lib_fail("set_option", st);
     if (!p.moduli.empty()) {
         const size_t vol = (size_t)g.nx * g.ny * g.nz;

@@ -56,7 +56,8 @@ def test_binary_roundtrip_and_checks(tmp_path):
 def test_driver_usage_errors(driver):
     r = subprocess.run([driver, "--help"], capture_output=True, text=True)
     assert r.returncode == 0 and "usage" in r.stdout
-    for bad in (["--precision", "f8"], ["--bogus", "1"], ["--snap-field", "nope"], ["--format", "xml"], ["--nt"]):
+    for bad in (["--precision", "f8"], ["--bogus", "1"], ["--snap-field", "nope"], ["--format", "xml"], ["--nt"],
+                ["--variant", "fast"]):
         r = subprocess.run([driver, *bad], capture_output=True, text=True)
         assert r.returncode == 1, bad
     r = subprocess.run([driver, "--preset", "nope", "--setup-only", "--out", "/tmp"], capture_output=True, text=True)

@@ -62,3 +62,16 @@ def test_driver_cube_preset_runs(driver, tmp_path):
     assert vz.shape == (256, 120) and p.shape == (256, 120)
     assert np.isfinite(vz).all() and np.abs(p).max() > 0
     assert bio.read(tmp_path / "sspro_60.bin").shape == (64, 64)
+
+
+def test_driver_variant_option(driver, tmp_path):
+    """--variant selects the tiled-kernel variant; the tensor-memory variants with and without the x-slab staging
+    give the same bits."""
+    out = {}
+    for v in ("tmem", "tmem_xs"):
+        d = tmp_path / v
+        meta = _run(driver, d, "--preset", "layered256", "--scale", "0.5", "--nt", "60", "--snap", "30",
+                    "--format", "binary", "--precision", "f16", "--variant", v)
+        assert meta["health_ok"]
+        out[v] = bio.read(d / "sis_vuz.bin")
+    np.testing.assert_array_equal(out["tmem"], out["tmem_xs"])
