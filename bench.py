@@ -272,7 +272,8 @@ def shots_leg(args):
     for n in sizes:
         s = behf.solver_for(shots.shot_problem(n, 1000 * n, nt), precision=args.precision)
         z, ms = s.autotune(3)
-        tuned[n] = {"variant": s.info()["tiled_variant"], "zchunk": z, "ms_per_step": ms}
+        tuned[n] = {"variant": s.info()["tiled_variant"], "tile_rows": s.info()["tile_rows"], "zchunk": z,
+                    "ms_per_step": ms}
         s.close()
         for i in range(per):
             s = behf.solver_for(shots.shot_problem(n, 1000 * n + i, nt), precision=args.precision)
@@ -285,6 +286,7 @@ def shots_leg(args):
             group = [behf.solver_for(shots.shot_problem(n, 1000 * n + i, nt), precision=args.precision)
                      for i in range(g0, min(per, g0 + batch))]
             for s in group:
+                s.set_option(behf.OPT_TILE_ROWS, tuned[n]["tile_rows"])
                 s.set_option(behf.OPT_TILED_VARIANT, behf.TILED_VARIANT[tuned[n]["variant"]])
                 s.set_option(behf.OPT_ZCHUNK, tuned[n]["zchunk"])
             l0 = sum(s.info()["launches"] for s in group)
@@ -400,6 +402,7 @@ def behf_arm(args, world, rank, local):
                                  "achieved": value / world * ab["step_fused"], "frac": value / world * ab["step_fused"] / peak,
                                  "roofline_gpts": peak / ab["step_fused"]},
                "kernel_ms": kt, "kernel_family": info["kernel"], "kernel_variant": info["tiled_variant"],
+               "tile_rows": info["tile_rows"],
                "scales": info["scales"], "health_ok": ok,
                "fp32": fp32, "fp16_over_fp32": (value / world / fp32["auto"]) if fp32 else None,
                "fp16_over_plain_fp32": (value / world / fp32["plain"]) if fp32 else None,

@@ -83,6 +83,7 @@ typedef struct {
     int tiled_variant;       /* tiled kernels in use: 1 classic, 2 warp-specialised, 3 warp-specialised + TMEM z,
                                 4 the same + x-slab CPML memory by TMA */
     int zchunk;              /* z planes per CTA requested for the tiled kernels (0 = automatic) */
+    int tile_rows;           /* rows per tile of the tiled kernels (8 or 4) */
 } behf_info;
 
 /* Kernel family: PLAIN = one thread per cell with cached neighbour loads; TILED = the z-marching
@@ -121,6 +122,9 @@ enum {
                                     accumulators sum each checkpoint segment in FP32, then fold it into running
                                     totals: 1 = Neumaier-compensated FP32 totals (default), 0 = no fold (plain FP32
                                     accumulation over all steps), 2 = FP64 totals (reference for the error) */
+    BEHF_OPT_TILE_ROWS = 13,     /* tiled kernels: rows per tile (each a warp), 0 = automatic (8), 8 or 4 (64 x 4 tiles: four
+                                    compute warps and a producer per CTA, up to four CTAs per SM); the autotuner
+                                    times both */
     BEHF_OPT_RECOMPUTE_OVERLAP = 12, /* gradient, one checkpoint level: 1 = the recompute of the next segment from its
                                     checkpoint runs on a second stream, into a second snapshot buffer, while the
                                     current segment's adjoint steps run (default; only when the second buffer fits
@@ -272,9 +276,11 @@ behf_status behf_physical_gradient(long long ncell, const float* const moduli[BE
                                    double* const grad_phys[BEHF_NPHYS]);
 
 /* Autotuner (no counterpart in the reference, which fixes its 16 x 8 block, kernel.cu:17-19): times trial_steps
- * steps for each tiled-kernel variant (BEHF_OPT_TILED_VARIANT 1..4) and each z-chunk length (BEHF_OPT_ZCHUNK
- * candidates 0, 16, 32, ... up to the grid), keeps the fastest pair, and resets the wavefields (behf_reset).
- * Writes the chosen z-chunk and its milliseconds per step; the chosen variant is in behf_info.tiled_variant. */
+ * steps for each tile height (BEHF_OPT_TILE_ROWS 8 and 4), tiled-kernel variant (BEHF_OPT_TILED_VARIANT 1..4) and
+ * z-chunk length (BEHF_OPT_ZCHUNK
+ * candidates 0, 16, 32, ... up to the grid), keeps the fastest, and resets the wavefields (behf_reset).
+ * Writes the chosen z-chunk and its milliseconds per step; the chosen variant and height are in
+ * behf_info.tiled_variant and behf_info.tile_rows. */
 behf_status behf_autotune(behf_ctx* ctx, int trial_steps, int* zchunk_out, double* ms_per_step_out);
 
 /* Batched shots on one GPU (no counterpart in the reference): advances n independent contexts by nsteps each,

@@ -25,7 +25,7 @@ SOURCE = {"explosive": 0, "pressure": 1, "force_z": 2}
 KERNEL = {"auto": 0, "plain": 1, "tiled": 2}
 (OPT_KERNEL, OPT_REF_BUG_COMPAT, OPT_GRAPH_CHUNK, OPT_GRADIENT, OPT_CHECKPOINT, OPT_ZCHUNK, OPT_COEF_ROUNDING,
  OPT_STATE_ROUNDING, OPT_SNAPSHOT_CACHE, OPT_CHECKPOINT_OUTER, OPT_TILED_VARIANT, OPT_GRAD_COMPENSATION,
- OPT_RECOMPUTE_OVERLAP) = range(13)
+ OPT_RECOMPUTE_OVERLAP, OPT_TILE_ROWS) = range(14)
 TILED_VARIANT = {"auto": 0, "classic": 1, "ws": 2, "tmem": 3, "tmem_xs": 4}
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "allocation failed", -4: "call out of order",
           -5: "non-finite or saturated field", -6: "unsupported"}
@@ -78,7 +78,7 @@ def medium_spec(layers, interfaces=(), seed=1234, corr_cells=10.0, pct=0.0, log_
 class Info(C.Structure):
     _fields_ = [("step", C.c_int64), ("device_bytes", C.c_int64), ("scales", C.c_double * 4),
                 ("bytes_per_cell", C.c_double), ("kernel", C.c_int), ("radius", C.c_int), ("precision", C.c_int),
-                ("launches", C.c_int64), ("tiled_variant", C.c_int), ("zchunk", C.c_int)]
+                ("launches", C.c_int64), ("tiled_variant", C.c_int), ("zchunk", C.c_int), ("tile_rows", C.c_int)]
 
 
 def lib_path() -> Path:
@@ -268,7 +268,7 @@ class Solver:
                 "bytes_per_cell": inf.bytes_per_cell, "kernel": {0: "auto", 1: "plain", 2: "tiled"}[inf.kernel],
                 "radius": inf.radius, "precision": inf.precision, "launches": inf.launches,
                 "tiled_variant": {1: "classic", 2: "ws", 3: "tmem", 4: "tmem_xs"}.get(inf.tiled_variant, "classic"),
-                "zchunk": inf.zchunk}
+                "zchunk": inf.zchunk, "tile_rows": inf.tile_rows}
 
     def update_wavelet(self, it0: int, w: np.ndarray):
         w = _f32(w)
@@ -288,8 +288,8 @@ class Solver:
         return {"source": ms[0], "velocity": ms[1], "stress": ms[2], "record": ms[3]}
 
     def autotune(self, trial_steps: int = 4):
-        """Pick the fastest tiled-kernel variant and z-chunk length; resets the wavefields.  Returns (zchunk, ms/step);
-        the variant is info()["tiled_variant"]."""
+        """Pick the fastest tile height, tiled-kernel variant and z-chunk length; resets the wavefields.  Returns
+        (zchunk, ms/step); the variant and height are info()["tiled_variant"] and info()["tile_rows"]."""
         z, ms = C.c_int(0), C.c_double(0)
         _check(self._lib.behf_autotune(self._ctx, int(trial_steps), C.byref(z), C.byref(ms)))
         return z.value, ms.value

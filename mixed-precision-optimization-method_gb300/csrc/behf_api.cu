@@ -133,6 +133,7 @@ struct behf_ctx {
     int nblk_health = 0;
     // tiled kernels: TMA descriptors (built once, the arrays never move) and the device error word
     bool tiled_ok = false;
+    int tile_rows = 8;    // tiled kernels: rows per tile (8, or 4: kernels_tiled_*_rows4.cu)
     tiled::VMaps* vmaps = nullptr;
     tiled::TMaps* tmaps = nullptr;
     int* d_err = nullptr;
@@ -191,18 +192,33 @@ namespace {
 template <class S>
 cudaError_t launch_update(behf_ctx* c, bool vel) {
     const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok;
-    if (tiled)
-        return launch_tiled<S>(c->g, c->p, vel ? (const void*)c->vmaps : (const void*)c->tmaps, vel, c->stream);
+    if (tiled) {
+        const void* maps = vel ? (const void*)c->vmaps : (const void*)c->tmaps;
+        return c->tile_rows == 4 ? launch_tiled_rows4<S>(c->g, c->p, maps, vel, c->stream)
+                                 : launch_tiled<S>(c->g, c->p, maps, vel, c->stream);
+    }
     return launch_plain<S>(c->g, c->p, vel, c->stream);
 }
 
+// The tiled kernels' tensor maps for the context's tile height (the two heights' maps have one layout; their boxes
+// differ), allocated on first use.
 template <class S>
 bool setup_tiled(behf_ctx* c) {
-    if (!tiled_supported<S>(c->g)) return false;
-    c->vmaps = static_cast<tiled::VMaps*>(std::aligned_alloc(64, (sizeof(tiled::VMaps) + 63) / 64 * 64));
-    c->tmaps = static_cast<tiled::TMaps*>(std::aligned_alloc(64, (sizeof(tiled::TMaps) + 63) / 64 * 64));
+    if (!(c->tile_rows == 4 ? tiled_supported_rows4<S>(c->g) : tiled_supported<S>(c->g))) return false;
+    if (!c->vmaps) c->vmaps = static_cast<tiled::VMaps*>(std::aligned_alloc(64, (sizeof(tiled::VMaps) + 63) / 64 * 64));
+    if (!c->tmaps) c->tmaps = static_cast<tiled::TMaps*>(std::aligned_alloc(64, (sizeof(tiled::TMaps) + 63) / 64 * 64));
     if (!c->vmaps || !c->tmaps) return false;
-    return tiled_build_maps<S>(c->g, c->p, c->vmaps, c->tmaps) == cudaSuccess;
+    return (c->tile_rows == 4 ? tiled_build_maps_rows4<S>(c->g, c->p, c->vmaps, c->tmaps)
+                              : tiled_build_maps<S>(c->g, c->p, c->vmaps, c->tmaps)) == cudaSuccess;
+}
+
+bool setup_tiled_any(behf_ctx* c) {
+    switch (c->prec) {
+        case BEHF_FP32: return setup_tiled<float>(c);
+        case BEHF_FP16: return setup_tiled<__half>(c);
+        case BEHF_BF16: return setup_tiled<__nv_bfloat16>(c);
+    }
+    return false;
 }
 
 cudaError_t dispatch_update(behf_ctx* c, bool vel) {
@@ -584,14 +600,7 @@ behf_status behf_create(const behf_grid* gr, int precision, behf_ctx** out) {
     g.step = c->d_it;
     if (st == BEHF_OK) st = upload_profiles(c);
     if (st == BEHF_OK) st = zero_state(c);
-    if (st == BEHF_OK) {
-        switch (precision) {
-            case BEHF_FP32: c->tiled_ok = setup_tiled<float>(c); break;
-            case BEHF_FP16: c->tiled_ok = setup_tiled<__half>(c); break;
-            case BEHF_BF16: c->tiled_ok = setup_tiled<__nv_bfloat16>(c); break;
-            default: c->tiled_ok = false;
-        }
-    }
+    if (st == BEHF_OK) c->tiled_ok = setup_tiled_any(c);
     if (st) {
         delete c;
         return st == BEHF_ERR_CUDA && g_err.empty() ? fail(st, "initialisation failed") : st;
@@ -947,6 +956,20 @@ behf_status behf_set_option(behf_ctx* c, int opt, int value) {
             if (value < 0 || value > 1) return fail(BEHF_ERR_INVALID, "recompute overlap must be 0 or 1");
             c->rc_overlap = value;
             break;
+        case BEHF_OPT_TILE_ROWS: {
+            const int rows = value == 0 ? 8 : value;
+            if (rows != 4 && rows != 8) return fail(BEHF_ERR_INVALID, "tile rows must be 0 (automatic), 4 or 8");
+            if (rows != c->tile_rows) {
+                const int old = c->tile_rows;
+                c->tile_rows = rows;
+                if (c->tiled_ok && !setup_tiled_any(c)) {  // keep the previous height if the new one cannot run
+                    c->tile_rows = old;
+                    setup_tiled_any(c);
+                    return fail(BEHF_ERR_INVALID, "%d-row tiles are not supported on this grid", rows);
+                }
+            }
+            break;
+        }
         case BEHF_OPT_TILED_VARIANT:
             if (value < 0 || value > 4) return fail(BEHF_ERR_INVALID, "tiled variant must be 0 .. 4");
             c->g.ws = value == 0 ? auto_variant(c->prec) : value - 1;
@@ -974,6 +997,7 @@ behf_status behf_get_info(behf_ctx* c, behf_info* out) {
     out->launches = c->launches;
     out->tiled_variant = c->g.ws + 1;
     out->zchunk = c->g.zchunk_req;
+    out->tile_rows = c->tile_rows;
     return BEHF_OK;
 }
 
@@ -1589,20 +1613,31 @@ behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double*
     std::vector<int> zc = {0};
     for (int z = 16; z < planes; z *= 2) zc.push_back(z);
     zc.push_back(planes);
-    // (variant, z chunk) pairs: the variants only where the tiled kernels run
-    std::vector<std::pair<int, int>> cand;
+    // (tile rows, variant, z chunk): the heights and variants only where the tiled kernels run
+    struct Cand {
+        int rows, v, z;
+    };
+    std::vector<Cand> cand;
     const bool tiled = c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok;
-    for (int v = tiled ? 0 : c->g.ws; v <= (tiled ? 3 : c->g.ws); v++)
-        for (int z : zc) cand.push_back({v, z});
+    for (int rows : {8, 4}) {
+        if (!tiled && rows != c->tile_rows) continue;
+        for (int v = tiled ? 0 : c->g.ws; v <= (tiled ? 3 : c->g.ws); v++)
+            for (int z : zc) cand.push_back({rows, v, z});
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     double best = 1e300;
-    int best_z = 0, best_v = c->g.ws;
+    int best_z = 0, best_v = c->g.ws, best_rows = c->tile_rows;
     behf_status st = BEHF_OK;
     const int nrec = c->nrec;
     c->nrec = 0;  // trial steps record nothing
-    for (auto [v, z] : cand) {
+    for (const Cand& cd : cand) {
+        const int v = cd.v, z = cd.z;
+        if (cd.rows != c->tile_rows) {  // the other height's tensor maps
+            c->tile_rows = cd.rows;
+            if (tiled && !setup_tiled_any(c)) continue;
+        }
         c->g.ws = v;
         c->g.zchunk_req = z;
         c->invalidate_graph();
@@ -1618,11 +1653,16 @@ behf_status behf_autotune(behf_ctx* c, int trial_steps, int* zchunk_out, double*
             best = ms / trial_steps;
             best_z = z;
             best_v = v;
+            best_rows = cd.rows;
         }
     }
     c->nrec = nrec;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (best_rows != c->tile_rows) {
+        c->tile_rows = best_rows;
+        if (tiled && !setup_tiled_any(c) && !st) st = fail(BEHF_ERR_CUDA, "tensor maps for %d-row tiles", best_rows);
+    }
     c->g.ws = best_v;
     c->g.zchunk_req = best_z;
     c->invalidate_graph();

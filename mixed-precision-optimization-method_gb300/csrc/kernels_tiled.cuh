@@ -22,8 +22,18 @@
 
 #include "behf_internal.cuh"
 
+// The tiled kernels are compiled twice: with 8-row tiles in behf::tiled (kernels_tiled_<type>.cu) and with 4-row
+// tiles in behf::tiled4, entry points suffixed _rows4 (kernels_tiled_<type>_rows4.cu).  A translation unit sets the
+// tile height, the namespace and the entry-point names before including this header.
+#ifndef BEHF_TILED_NAMESPACE
+#define BEHF_TILED_NAMESPACE tiled
+#endif
+#ifndef BEHF_TILED_FN
+#define BEHF_TILED_FN(name) name
+#endif
+
 namespace behf {
-namespace tiled {
+namespace BEHF_TILED_NAMESPACE {
 
 #ifndef BEHF_TILED_TY
 #define BEHF_TILED_TY 8
@@ -366,5 +376,5 @@ __device__ __forceinline__ float pml1(float D, float* psi, float* prv, float A, 
     return D + pn;
 }
 
-}  // namespace tiled
+}  // namespace BEHF_TILED_NAMESPACE
 }  // namespace behf

@@ -14,4 +14,16 @@ template <>
 cudaError_t launch_tiled<double>(const Geom&, const DevPtrs&, const void*, bool, cudaStream_t) {
     return cudaErrorNotSupported;
 }
+template <>
+bool tiled_supported_rows4<double>(const Geom&) {
+    return false;
+}
+template <>
+cudaError_t tiled_build_maps_rows4<double>(const Geom&, const DevPtrs&, void*, void*) {
+    return cudaErrorNotSupported;
+}
+template <>
+cudaError_t launch_tiled_rows4<double>(const Geom&, const DevPtrs&, const void*, bool, cudaStream_t) {
+    return cudaErrorNotSupported;
+}
 }  // namespace behf

@@ -4,7 +4,7 @@
 #include "kernels_tiled.cuh"
 
 namespace behf {
-namespace tiled {
+namespace BEHF_TILED_NAMESPACE {
 
 // Pipeline depth: NS stages in the shared-memory ring (NS - 1 planes in flight while one is computed), and
 // the CTAs per SM the launch bounds aim for (registers capped at 65536 / (256 MINB)).
@@ -685,14 +685,14 @@ __global__ void __launch_bounds__(NTH, Depth<S>::MINB_T)
     if (tid == 0) producer_drain<M>(pp);
 }
 
-}  // namespace tiled
+}  // namespace BEHF_TILED_NAMESPACE
 }  // namespace behf
 
 #include "kernels_tiled_ws.cuh"
 #include "kernels_tiled_zq.cuh"
 
 namespace behf {
-namespace tiled {
+namespace BEHF_TILED_NAMESPACE {
 
 // ----------------------------------------------------------------------------------------- host side
 template <class S, int R>
@@ -839,33 +839,33 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
     return cudaGetLastError();
 }
 
-}  // namespace tiled
+}  // namespace BEHF_TILED_NAMESPACE
 
 #define BEHF_TILED_INSTANTIATE(S)                                                                           \
     template <>                                                                                            \
-    bool tiled_supported<S>(const Geom& g) {                                                               \
-        return g.R >= 1 && g.R <= 4 && tiled::encoder() != nullptr && g.nz > 2 * g.R;                      \
+    bool BEHF_TILED_FN(tiled_supported)<S>(const Geom& g) {                                                               \
+        return g.R >= 1 && g.R <= 4 && BEHF_TILED_NAMESPACE::encoder() != nullptr && g.nz > 2 * g.R;                      \
     }                                                                                                      \
     template <>                                                                                            \
-    cudaError_t tiled_build_maps<S>(const Geom& g, const DevPtrs& p, void* vm, void* tm) {                 \
+    cudaError_t BEHF_TILED_FN(tiled_build_maps)<S>(const Geom& g, const DevPtrs& p, void* vm, void* tm) {                 \
         bool ok = false;                                                                                   \
-        auto* v = reinterpret_cast<tiled::VMaps*>(vm);                                                     \
-        auto* t = reinterpret_cast<tiled::TMaps*>(tm);                                                     \
+        auto* v = reinterpret_cast<BEHF_TILED_NAMESPACE::VMaps*>(vm);                                                     \
+        auto* t = reinterpret_cast<BEHF_TILED_NAMESPACE::TMaps*>(tm);                                                     \
         switch (g.R) {                                                                                     \
-            case 1: ok = tiled::build_maps_r<S, 1>(g, p, v, t); break;                                      \
-            case 2: ok = tiled::build_maps_r<S, 2>(g, p, v, t); break;                                      \
-            case 3: ok = tiled::build_maps_r<S, 3>(g, p, v, t); break;                                      \
-            case 4: ok = tiled::build_maps_r<S, 4>(g, p, v, t); break;                                      \
+            case 1: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 1>(g, p, v, t); break;                                      \
+            case 2: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 2>(g, p, v, t); break;                                      \
+            case 3: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 3>(g, p, v, t); break;                                      \
+            case 4: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 4>(g, p, v, t); break;                                      \
         }                                                                                                  \
         return ok ? cudaSuccess : cudaErrorInvalidValue;                                                   \
     }                                                                                                      \
     template <>                                                                                            \
-    cudaError_t launch_tiled<S>(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) { \
+    cudaError_t BEHF_TILED_FN(launch_tiled)<S>(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st) { \
         switch (g.R) {                                                                                     \
-            case 1: return tiled::launch_r<S, 1>(g, p, maps, vel, st);                                      \
-            case 2: return tiled::launch_r<S, 2>(g, p, maps, vel, st);                                      \
-            case 3: return tiled::launch_r<S, 3>(g, p, maps, vel, st);                                      \
-            case 4: return tiled::launch_r<S, 4>(g, p, maps, vel, st);                                      \
+            case 1: return BEHF_TILED_NAMESPACE::launch_r<S, 1>(g, p, maps, vel, st);                                      \
+            case 2: return BEHF_TILED_NAMESPACE::launch_r<S, 2>(g, p, maps, vel, st);                                      \
+            case 3: return BEHF_TILED_NAMESPACE::launch_r<S, 3>(g, p, maps, vel, st);                                      \
+            case 4: return BEHF_TILED_NAMESPACE::launch_r<S, 4>(g, p, maps, vel, st);                                      \
         }                                                                                                  \
         return cudaErrorInvalidValue;                                                                      \
     }

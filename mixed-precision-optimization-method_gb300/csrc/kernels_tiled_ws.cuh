@@ -11,7 +11,7 @@
 #pragma once
 
 namespace behf {
-namespace tiled {
+namespace BEHF_TILED_NAMESPACE {
 
 #ifndef BEHF_WS_NS
 #define BEHF_WS_NS 2
@@ -375,5 +375,5 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     if (failed) atomicExch(g.err, 1);
 }
 
-}  // namespace tiled
+}  // namespace BEHF_TILED_NAMESPACE
 }  // namespace behf

@@ -14,7 +14,8 @@
 //   bwd  D(k) = sum_m c_m (f(k+m-1) - f(k-m)):  D(z-R) is complete before f(z) arrives; f(z) adds
 //        +c_{R-j+1} (j <= R) / -c_{j-R} (j > R) to D(z-R+j), j = 1..2R.
 // Each CTA allocates 128 TMEM columns (warps w and w + 4 share a 32-lane quarter, 64 columns each: 4 fields x 16);
-// the register limit keeps at most two such CTAs on an SM (256 of the 512 columns), so an allocation never waits.
+// the register limit keeps at most two 8-row CTAs (or four 4-row CTAs of 64 columns) on an SM, 256 of the 512
+// columns, so an allocation never waits.
 // The first 2R planes of a z range arrive in a one-shot warm-up area, whose partial sums are formed in registers;
 // once every compute warp has read it, the tiles at the x edges receive there, with each plane, the CPML memory of
 // their x-slab cells (TMA boxes), so that their slab updates read it from shared memory instead of waiting on
@@ -24,7 +25,7 @@
 #include <type_traits>
 
 namespace behf {
-namespace tiled {
+namespace BEHF_TILED_NAMESPACE {
 
 #ifndef BEHF_ZQ_NS
 #define BEHF_ZQ_NS 2
@@ -40,7 +41,7 @@ constexpr int kZqUnroll = BEHF_ZQ_UNROLL;
 #ifndef BEHF_ZQ_PAIRYZ
 #define BEHF_ZQ_PAIRYZ true
 #endif
-constexpr uint32_t kZqCols = 128;  // TMEM columns per CTA
+constexpr uint32_t kZqCols = 16 * TY;  // TMEM columns per CTA: 64 per lane quarter's warps (TY / 4 of them)
 
 // Store a cell pair; FULL: both cells are known to be updated (no per-cell guard).
 template <class S, bool FULL>
@@ -180,7 +181,12 @@ struct ZMap {
 // (one set per stage).  Bytes of one set, and whether this CTA stages (CTA-uniform; xbase from xs_tile_base).
 // After the sets, the tile's four x profiles (TXC values each), brought once with the first plane.
 constexpr int kXsProfBytes = 4 * TXC * 4;
-__host__ __device__ __forceinline__ int xs_set_bytes(const Geom& g) { return 8 * g.xs_bw * TY * 4; }
+// Each array's box starts on a 128-byte boundary (the TMA rule for a shared-memory destination): with 8-row tiles
+// xs_bw x 8 x 4 bytes already is a multiple of 128, with 4-row tiles it is padded.  xs_set_tx: the bytes the eight
+// boxes bring (the stage's expected transaction count).
+__host__ __device__ __forceinline__ int xs_box_bytes(const Geom& g) { return al128(g.xs_bw * TY * 4); }
+__host__ __device__ __forceinline__ int xs_set_bytes(const Geom& g) { return 8 * xs_box_bytes(g); }
+__host__ __device__ __forceinline__ int xs_set_tx(const Geom& g) { return 8 * g.xs_bw * TY * 4; }
 template <class M>
 __device__ __forceinline__ bool xs_staged(const Geom& g, int xbase) {
     return xbase >= 0 && M::NS * xs_set_bytes(g) + kXsProfBytes <= M::bytes - M::warm;
@@ -306,7 +312,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
-                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xsb + (k == kb ? kXsProfBytes : 0)) : 0u));
+                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xs_set_tx(g) + (k == kb ? kXsProfBytes : 0)) : 0u));
                 tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0, k);      // txx  (x halo)
                 tma3(b + M::halo(1), &maps.halo[1], br, x0, y0 - R, k);          // tyy  (y halo)
                 tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // txy  (x, y halo)
@@ -326,7 +332,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             auto issue_x = [&](int st, int k) {
                 unsigned char* xb = smem + M::warm + st * xsb;
 #pragma unroll
-                for (int j = 0; j < 8; j++) tma3(xb + j * (xsb / 8), &maps.xs[j], &bfull[st], xbase, y0, k);
+                for (int j = 0; j < 8; j++) tma3(xb + j * xs_box_bytes(g), &maps.xs[j], &bfull[st], xbase, y0, k);
             };
             auto issue_p = [&]() {  // on the first plane's stage (stage 0)
                 unsigned char* pb = smem + M::warm + NS * xsb;
@@ -434,7 +440,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                     XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {true, true, false, false};
                 pml_pair<0, false, XS, BEHF_ZQ_PAIRYZ>(g, p, x, y, k, a0, a1, x1, s1, y2, z2, hf, y1, s2, x2, z3, hf, z1, s3, x3, y3, hf,
-                                       xrow, xbase, g.xs_bw * TY, xprof);
+                                       xrow, xbase, xs_box_bytes(g) / 4, xprof);
             }
             const float2 sum[3] = {add2(add2(x1, x2), x3), add2(add2(y1, y2), y3), add2(add2(z1, z2), z3)};
             const float2 dp[3] = {s1, s2, s3};
@@ -530,7 +536,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             auto issue = [&](int st, int k) {
                 unsigned char* b = smem + st * M::stage;
                 uint64_t* br = &bfull[st];
-                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xsb + (k == kb ? kXsProfBytes : 0)) : 0u));
+                mbar_expect_tx(br, M::stage_tx + (xs ? (uint32_t)(xs_set_tx(g) + (k == kb ? kXsProfBytes : 0)) : 0u));
                 tma3(b + M::halo(0), &maps.halo[0], br, x0 - G::HX, y0 - R, k);  // vx (x, y halo)
                 tma3(b + M::halo(1), &maps.halo[1], br, x0 - G::HX, y0 - R, k);  // vy
                 tma3(b + M::halo(2), &maps.halo[2], br, x0 - G::HX, y0 - R, k);  // vz
@@ -547,7 +553,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
             auto issue_x = [&](int st, int k) {
                 unsigned char* xb = smem + M::warm + st * xsb;
 #pragma unroll
-                for (int j = 0; j < 8; j++) tma3(xb + j * (xsb / 8), &maps.xs[j], &bfull[st], xbase, y0, k);
+                for (int j = 0; j < 8; j++) tma3(xb + j * xs_box_bytes(g), &maps.xs[j], &bfull[st], xbase, y0, k);
             };
             auto issue_p = [&]() {  // on the first plane's stage (stage 0)
                 unsigned char* pb = smem + M::warm + NS * xsb;
@@ -651,7 +657,7 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
                     XS ? reinterpret_cast<const float*>(smem + M::warm + NS * xs_set_bytes(g)) + xl : nullptr;
                 const bool hf[4] = {false, false, true, true};
                 pml_pair<4, false, XS, BEHF_ZQ_PAIRYZ>(g, p, x, y, k, a0, a1, uxx, wx, uyx, uzx, hf, uyy, wy, uxy, uzy, hf, uzz, wz, uxz,
-                                       uyz, hf, xrow, xbase, g.xs_bw * TY, xprof);
+                                       uyz, hf, xrow, xbase, xs_box_bytes(g) / 4, xprof);
             }
             const float2 dv = add2(add2(uxx, uyy), uzz);
             const float2 dq = add2(add2(wx, wy), wz);
@@ -693,5 +699,5 @@ __global__ void __launch_bounds__(NTH_WS, WDepth<S>::MINB)
     }
 }
 
-}  // namespace tiled
+}  // namespace BEHF_TILED_NAMESPACE
 }  // namespace behf

@@ -255,28 +255,34 @@ def test_tiled_half_kinds_match_oracle(behf_lib, oracle, precision):
 @pytest.mark.parametrize("radius", [1, 2, 4])
 @pytest.mark.parametrize("precision", ["f16", "bf16", "f32"])
 def test_tiled_variants(behf_lib, oracle, precision, radius):
-    """The four tiled-kernel variants on an odd grid with CPML whose x-edge tiles the fourth variant stages (their
-    x-slab CPML memory and profiles by TMA): every variant meets the parity bar against the FP64 oracle, and the
-    tensor-memory kernels with and without the staging give the same bits (only where that memory is read from
-    differs)."""
+    """The four tiled-kernel variants, with 8- and 4-row tiles, on an odd grid with CPML whose x-edge tiles the
+    fourth variant stages (their x-slab CPML memory and profiles by TMA): every variant meets the parity bar against
+    the FP64 oracle; the tensor-memory kernels with and without the staging give the same bits (only where that
+    memory is read from differs), and so do both tile heights of every variant (the per-cell arithmetic does not
+    depend on the tile)."""
     import behf
     prob = _odd_problem((150, 20, 36), radius, nt=80, cpml=8)  # x tiles at 0, 64, 128: both slabs staged
     ref, _ = oracle.run(prob, "f64")
     out = {}
+    for rows in (8, 4):
+        for v in (1, 2, 3, 4):
+            s = behf.solver_for(prob, precision=precision, kernel="tiled")
+            s.set_option(behf.OPT_TILE_ROWS, rows)
+            s.set_option(behf.OPT_TILED_VARIANT, v)
+            s.run(prob.nt)
+            out[rows, v] = s.seismograms()
+            info = s.info()
+            assert info["tiled_variant"] == ["classic", "ws", "tmem", "tmem_xs"][v - 1] and info["tile_rows"] == rows
+            ok, _ = s.health()
+            s.close()
+            assert ok
+            errs = _per_field_err(oracle, prob, out[rows, v], ref)
+            for comp, e in errs.items():
+                tol = TOL_Q[precision] if precision in TOL_Q and comp in (3, 4, 5) else TOL[precision]
+                assert e < tol, (rows, v, comp, errs)
+        np.testing.assert_array_equal(out[rows, 3], out[rows, 4])
     for v in (1, 2, 3, 4):
-        s = behf.solver_for(prob, precision=precision, kernel="tiled")
-        s.set_option(behf.OPT_TILED_VARIANT, v)
-        s.run(prob.nt)
-        out[v] = s.seismograms()
-        assert s.info()["tiled_variant"] == ["classic", "ws", "tmem", "tmem_xs"][v - 1]
-        ok, _ = s.health()
-        s.close()
-        assert ok
-        errs = _per_field_err(oracle, prob, out[v], ref)
-        for comp, e in errs.items():
-            tol = TOL_Q[precision] if precision in TOL_Q and comp in (3, 4, 5) else TOL[precision]
-            assert e < tol, (v, comp, errs)
-    np.testing.assert_array_equal(out[3], out[4])
+        np.testing.assert_array_equal(out[4, v], out[8, v])
 
 
 @pytest.mark.parametrize("precision", ["f32", "f16"])
