@@ -252,16 +252,18 @@ def test_tiled_half_kinds_match_oracle(behf_lib, oracle, precision):
     s.close()
 
 
-@pytest.mark.parametrize("radius", [1, 2, 4])
+@pytest.mark.parametrize("shape", [(150, 20, 36), (128, 24, 40)])
+@pytest.mark.parametrize("radius", [1, 2, 3, 4])
 @pytest.mark.parametrize("precision", ["f16", "bf16", "f32"])
-def test_tiled_variants(behf_lib, oracle, precision, radius):
+def test_tiled_variants(behf_lib, oracle, precision, radius, shape):
     """The four tiled-kernel variants, with 8- and 4-row tiles, on an odd grid with CPML whose x-edge tiles the
     fourth variant stages (their x-slab CPML memory and profiles by TMA): every variant meets the parity bar against
     the FP64 oracle; the tensor-memory kernels with and without the staging give the same bits (only where that
     memory is read from differs), and so do both tile heights of every variant (the per-cell arithmetic does not
-    depend on the tile)."""
+    depend on the tile).  nx = 150: x tiles at 0, 64, 128, both slabs staged; nx = 128 (a multiple of 4): the y/z
+    slab memory also has the tensor maps that variant 3's producer prefetches through."""
     import behf
-    prob = _odd_problem((150, 20, 36), radius, nt=80, cpml=8)  # x tiles at 0, 64, 128: both slabs staged
+    prob = _odd_problem(shape, radius, nt=80, cpml=8)
     ref, _ = oracle.run(prob, "f64")
     out = {}
     for rows in (8, 4):
