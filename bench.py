@@ -19,6 +19,7 @@ on a bounded sample of the same workload (a 160^3 grid of the same medium and sc
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -56,6 +57,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="behf", choices=["behf", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="grid cells per axis")
+    ap.add_argument("--nx", type=int, default=0, help="diagnostics: x extent of a narrower grid (0: n); nx = 128 makes "
+                    "every x tile an x-edge tile")
     ap.add_argument("--cpml", type=int, default=20, help="CPML cells per face (20 at 1024^3; 7 at 384^3 gives the "
                     "same slab fraction of the grid)")
     ap.add_argument("--precision", default="f16", choices=["f16", "bf16", "f32", "f64"])
@@ -175,9 +178,11 @@ def reference_arm(args, world, rank):
 
 
 def config_dict(args):
-    return {"workload": f"random{args.n}: {args.n}^3 cells, h=5 m, dt=0.4 ms, radius 4, {args.cpml}-cell CPML, "
+    nx = args.nx or args.n
+    shape = f"{args.n}^3" if nx == args.n else f"{nx}x{args.n}x{args.n}"
+    return {"workload": f"random{args.n}: {shape} cells, h=5 m, dt=0.4 ms, radius 4, {args.cpml}-cell CPML, "
                         "5% Gaussian-correlated sandstone, force source 20 Hz, 512x512 receivers (vz,p)",
-            "grid": [args.n] * 3, "storage": args.precision, "kernel": args.kernel,
+            "grid": [nx, args.n, args.n], "storage": args.precision, "kernel": args.kernel,
             "parallelism": f"replicas x{args.gpus}", "l2": "no flush: working set ~96 GB >> 129 MB L2"}
 
 
@@ -319,6 +324,11 @@ def behf_arm(args, world, rank, local):
     e2e_steps = 0 if args.no_e2e else max(args.steps // 2, 3)
     total = args.warmup + args.steps + ktime + e2e_steps
     prob = problems.random1024(n=n, nt=total, medium=False, cpml=args.cpml)
+    nx = args.nx or n
+    if nx != n:  # a narrower grid: the x extent cut, the source and receivers moved inside it
+        ijk = prob.rec_ijk.copy()
+        ijk[:, 0] = np.clip(ijk[:, 0], args.cpml + 2, nx - args.cpml - 3)
+        prob = dataclasses.replace(prob, nx=nx, src=(nx // 2,) + tuple(prob.src[1:]), rec_ijk=ijk)
     cells = prob.cells
     s = make_solver(prob, args.precision, args.kernel, total)
     s.run(args.warmup)
@@ -331,7 +341,7 @@ def behf_arm(args, world, rank, local):
 
     # per-kernel durations (CUDA events around each launch, on the library's stream)
     kt = s.time_kernels(ktime)
-    ab = behf.algorithmic_bytes(args.precision, (n, n, n), prob.cpml_width)
+    ab = behf.algorithmic_bytes(args.precision, (nx, n, n), prob.cpml_width)
     dom = "velocity" if kt["velocity"] >= kt["stress"] else "stress"
     peak, peak_kind = peak_hbm()
     achieved = ab[dom] * cells / (kt[dom] * 1e-3) / 1e9
