@@ -11,7 +11,8 @@ the relative L2 of each of the 13 final wavefields.
         bug-compatible vz, the reference's storage scales, txx on the vertical line through the source):
         FP64 vs FP32, FP16, BF16 (automatic scales; --ref-scales: the reference's 1e8, 1e8, 1, 1)
 
-Prints one JSON object: per precision and per recorded field the relative L2 error of all traces, per
+Prints one JSON object: per precision and per recorded field the relative L2 error of all traces (and in the
+signal band, both traces low-passed at 4 f0), per
 wavefield the relative L2 error of the field after nt/4, nt/2 and nt steps (physical units, read back as float32;
 `field_rel_l2` is the final one; with the reference's field norms at those steps, since a field whose waves have
 left through the CPML is a small residue whose relative error says little; skipped at 1024^3, where 13 fields are
@@ -55,6 +56,13 @@ def run_one(prob, precision: str, kernel: str = "auto", coef_rounding: int = 0, 
     s.close()
     return seis, {"wall_s": wall, "health_ok": bool(ok), "kernel": info["kernel"], "scales": info["scales"],
                   "gpts": prob.cells * prob.nt / wall / 1e9}, snaps if fields else None
+
+
+def lowpass(x: np.ndarray, dt: float, fc: float) -> np.ndarray:
+    """Zero-phase low-pass of each trace (rows): the FFT bins above fc set to zero."""
+    X = np.fft.rfft(x, axis=1)
+    X[:, np.fft.rfftfreq(x.shape[1], dt) > fc] = 0
+    return np.fft.irfft(X, n=x.shape[1], axis=1)
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
@@ -108,6 +116,10 @@ def main(argv=None):
                                     state_rounding=args.state_rounding, scale_boost=args.scale_boost, fields=fields,
                                     scales=scales)
         meta["rel_l2"] = {FIELDS[c]: rel_l2(seis[prob.rec_comp == c], ref[prob.rec_comp == c]) for c in comps}
+        # the same in the signal band (both traces low-passed at 4 f0, which keeps the reference's energy)
+        fc = 4 * prob.f0
+        meta["rel_l2_band"] = {FIELDS[c]: rel_l2(lowpass(seis[prob.rec_comp == c], prob.dt, fc),
+                                                 lowpass(ref[prob.rec_comp == c], prob.dt, fc)) for c in comps}
         if fields:
             meta["field_rel_l2_at"] = {m: {name: rel_l2(final[m][name], ref_fields[m][name]) for name in FIELDS}
                                        for m in ref_fields}

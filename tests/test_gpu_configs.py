@@ -8,8 +8,8 @@ layered256 (256^3, 2000 steps, 20-cell CPML, sandstone over the stiff layer at z
 16 x 16 surface receivers recording vz and p) against the GPU FP64 run of the same scheme (the plain kernels,
 which the parity tests pin to the CPU oracle within 1e-10):
     FP32 storage (tiled and plain kernels)   <= 1e-4
-    FP16 storage, raw traces                 <= 2.5e-2  (measured 2.2e-2 / 2.3e-2: above the 2e-2 bar)
-    FP16 storage, signal band (<= 4 f0)      <= 2e-2    (measured 4.7e-3 / 7.0e-3)
+    FP16 storage, raw traces                 <= 2.5e-2  (measured 2.3e-2 / 2.3e-2: above the 2e-2 bar)
+    FP16 storage, signal band (<= 4 f0)      <= 2e-2    (measured 4.8e-3 / 7.4e-3)
 The FP16 excess over 2e-2 is grid-scale noise from rounding the stored stresses (the oracle's per-field rounding
 emulation puts 93 % of the error on the six stresses): 95 % of its energy lies between 100 and 800 Hz, where the
 FP64 traces hold none, and a third of it arrives after the pulse has passed.  The signal-band figure compares both
