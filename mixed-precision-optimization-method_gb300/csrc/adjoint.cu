@@ -62,6 +62,12 @@ struct Adj {
         return (A)reinterpret_cast<const W*>(p.k[VW1X + a])[o];
     }
     static __device__ __forceinline__ A prof(const void* v, int i) { return reinterpret_cast<const A*>(v)[i]; }
+    // L2 prefetch of element o of an array of element type E (no register is written: the plane's loads that
+    // follow find the line in L2 instead of waiting on DRAM)
+    template <class E>
+    static __device__ __forceinline__ void pf(const void* f, long long o) {
+        asm volatile("prefetch.L2 [%0];" ::"l"(reinterpret_cast<const E*>(f) + o));
+    }
 
 };
 
@@ -462,10 +468,64 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
         issue(0, kb, true);
         pend = 1u;
     }
+    // Own-cell arrays of plane kn (the ones the loads of the cell body below read from global memory, under the
+    // same conditions) prefetched into L2 one plane ahead: the stencil inputs arrive by TMA, and without this
+    // every plane's own loads wait on DRAM latency with nothing else in flight.
+    typedef typename Traits<S>::K K;
+    typedef typename Traits<S>::W Wt;
+    auto prefetch_plane = [&](int kn) {
+        const long long cn = kn * sz + j * sy + i;
+        const bool inn = interior(g, i, j, kn);
+        if constexpr (MODE == 2) {
+            if (!(a.grad && inn)) return;
+            if constexpr (KIND == 0) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    Q::template pf<A>(a.mu[d], cn);
+                    Q::template pf<A>(a.lf[BEHF_VX + d], cn);
+                    Q::template pf<S>(a.qprev[d], cn);
+                    Q::template pf<S>(a.cur[BEHF_QX + d], cn);
+                    if (a.derived) {
+                        Q::template pf<K>(p.k[VU2X + d], cn);
+                        Q::template pf<K>(p.k[VW3X + d], cn);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 15; q++)
+                    if (!(a.derived && q >= VW2X && q <= VW2Z)) Q::template pf<A>(a.g[q], cn);
+            } else {
+                if (!fuse) return;
+#pragma unroll
+                for (int q = 0; q < 7; q++) Q::template pf<A>(a.lf[BEHF_SXX + q], cn);
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    if (q != 4 || !a.derived) Q::template pf<A>(a.g[P1 + q], cn);
+            }
+        } else if constexpr (KIND == 0) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                Q::template pf<A>(a.lf[BEHF_VX + d], cn);
+                Q::template pf<A>(a.lf[BEHF_QX + d], cn);
+                Q::template pf<K>(p.k[VU2X + d], cn);
+                Q::template pf<Wt>(p.k[VW1X + d], cn);
+                Q::template pf<K>(p.k[VU1X + d], cn);
+                Q::template pf<K>(p.k[VW3X + d], cn);
+                if (!a.derived) Q::template pf<K>(p.k[VW2X + d], cn);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 7; q++) Q::template pf<A>(a.lf[BEHF_SXX + q], cn);
+            if (fuse)
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    if (q != 4 || !a.derived) Q::template pf<K>(p.k[P1 + q], cn);
+        }
+    };
     bool failed = false;
     for (int k = kb, it = 0; k < ke; k++, it++) {
         const int st = it & 1;
         bool ok = true;
+        if (a.pf && valid && k + 1 < ke) prefetch_plane(k + 1);
         if (tid == 0 && k + 1 < ke) {
             const int sn = st ^ 1;
             if (it >= 1) {  // stage sn was read in iteration it - 1: wait until every warp released it

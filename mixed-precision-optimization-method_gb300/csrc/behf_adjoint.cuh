@@ -34,6 +34,7 @@ struct AdjPtrs {
     int grad;                // accumulate coefficient gradients
     int derived;             // the forward ran the tiled kernels: VW2 = VU2 VW3 c_vw2, S3 = P1 c_s3 (the stored
                              // VW2 and S3 are not read, their gradients go to VU2, VW3 and P1)
+    int pf;                  // gathers and gradient kernels: prefetch each cell's own arrays of the next plane into L2
 };
 
 // Tensor maps of the twelve staged arrays of one gather (x windows, y windows, z-ring rows; adjoint.cu), and of

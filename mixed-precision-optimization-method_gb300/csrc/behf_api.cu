@@ -1198,6 +1198,10 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
     a.grad = 1;
     a.derived = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? 1 : 0;
+    {  // L2 prefetch in the adjoint kernels: on unless BEHF_ADJ_PREFETCH=0 (a diagnostic switch; same results)
+        const char* e = getenv("BEHF_ADJ_PREFETCH");
+        a.pf = (e && e[0] == '0') ? 0 : 1;
+    }
     // compensated summation of the FP32 accumulators: segment sums folded into running totals
     AdjFold fold{};
     const bool folding = sizeof(A) == 4 && c->grad_comp > 0;
