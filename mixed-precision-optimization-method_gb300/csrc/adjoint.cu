@@ -284,6 +284,40 @@ constexpr int GX = 32, GY = 8;
 #define BEHF_ADJ_MINB_G1 3
 #endif
 
+// The adjoint CPML memory update of one cell on every slab axis that holds it: k_vmem<A, TSLOT>'s work for that
+// cell, in a tile kernel (the gradient kernels do it for the slab cells of their tiles).  TSLOT 1: the T slots 4..7
+// from tmpT; TSLOT 0: the V slots 0..3 from tmpV.  Slot order and half-shifted profiles as in k_vmem.
+template <class A, int TSLOT>
+__device__ __forceinline__ void vmem_cell(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int i, int j, int k,
+                                          long long c) {
+    constexpr int ND = TSLOT ? 7 : 6, SB = TSLOT ? 4 : 0;
+    A d[ND];
+#pragma unroll
+    for (int q = 0; q < ND; q++) d[q] = reinterpret_cast<const A*>(TSLOT ? a.tmpT[q] : a.tmpV[q])[c];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        const int pos = ax == 0 ? i : ax == 1 ? j : k;
+        const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
+        if (s < 0) continue;
+        const long long so = slab_off(g, ax, i, j, k, s);
+        const int dq[4] = {ax, TSLOT ? 3 : ax + 3, TSLOT ? (ax == 2 ? 5 : 4) : (ax == 0 ? 1 : 0),
+                           TSLOT ? (ax == 0 ? 5 : 6) : (ax == 2 ? 1 : 2)};
+        A L[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) L[q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[so];
+        const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
+        const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const bool h = TSLOT ? q >= 2 : q < 2;
+            const A Ap = h ? pa2 : pa, B = h ? pb2 : pb;
+            const A Lm = L[q] + d[dq[q]];
+            reinterpret_cast<A*>(a.lpsi[ax][SB + q])[so] = Ap * Lm;
+            reinterpret_cast<A*>(a.lprv[ax][SB + q])[so] = Ap * B * Lm;
+        }
+    }
+}
+
 struct StageSet {
     int slot[3][4];  // [axis][array]: adjoint CPML memory slot and half-shift flag of each staged array
     int half[3][4];
@@ -393,7 +427,7 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                                        : KIND == 1                ? BEHF_ADJ_MINB_G1
                                                                   : BEHF_ADJ_MINB_SPLIT)
     k_gather(const __grid_constant__ GatherMaps maps, const __grid_constant__ GatherMaps smaps, Geom g, DevPtrs p,
-             AdjPtrs a, StageSet ss, int zc, int fuse) {
+             AdjPtrs a, StageSet ss, int zc, int fuse, int vmem) {
     typedef GatherOps<S, R> W;
     typedef Adj<S, R> Q;
     typedef GMap<S, R, MODE> M;
@@ -423,7 +457,12 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
     auto has_int = [&](int lo, int hi, int n) { return g.W == 0 || max(lo, g.L) <= min(hi, n - 2 - g.L); };
     const bool snap = M::SNAP && a.grad && (KIND == 0 || fuse) && has_int(i0, i0 + GX - 1, g.nx) &&
                       has_int(j0, j0 + GY - 1, g.ny) && has_int(kb, ke - 1, g.nz);
-    if (MODE == 2 && !snap) return;  // a gradient CTA without cells outside the slabs has nothing to do
+    if (MODE == 2 && !snap) {  // a gradient CTA without cells outside the slabs: at most the memory update
+        if (vmem && valid)
+            for (int k = kb; k < ke; k++)
+                vmem_cell<A, KIND == 0 ? 1 : 0>(g, p, a, i, j, k, k * g.plane + j * (long long)g.px + i);
+        return;
+    }
     // block-uniform: does the x (y) window of this tile reach a CPML slab of its axis?
     const bool cx = M::TMP && g.W > 0 && (i0 - R < g.L || i0 + GX + R > g.nx - 1 - g.L);
     const bool cy = M::TMP && g.W > 0 && (j0 - R < g.L || j0 + GY + R > g.ny - 1 - g.L);
@@ -731,6 +770,8 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                         t_stencils(sum, dp);
                         v_grad(go, mu, lv, qo, qn, sum, dp, vu2, vw3);
                         store_vgo(go);
+                    } else if (vmem && !inner) {  // the T-slot memory update of step n on the slab cells
+                        vmem_cell<A, 1>(g, p, a, i, j, k, c);
                     }
                 } else {  // T-coefficient gradients of step n - 1 (the stress/pressure adjoints the gather left)
                     if (fuse && a.grad && inner) {
@@ -740,6 +781,8 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                         load_tgo(go);
                         v_stencils(du);
                         store_tgo(lt, du, go);
+                    } else if (vmem && !inner) {  // the V-slot memory update of step n on the slab cells
+                        vmem_cell<A, 0>(g, p, a, i, j, k, c);
                     }
                 }
             } else if constexpr (KIND == 0) {
@@ -1132,12 +1175,16 @@ cudaError_t adj_r(const Geom& g, const DevPtrs& p, const AdjPtrs& a, const AdjMa
     // T^T gather + V^T; its V-coefficient gradients; V^T gather + T-slot memory + T^T of step n - 1; its
     // T-coefficient gradients
     typedef typename Traits<S>::C A;
-    k_gather<S, R, 0, MG><<<ggrid, block, smemg, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0);
-    if (split && a.grad) k_gather<S, R, 0, 2><<<ggrid, block, smemd, st>>>(m.t, *snapT, g, p, a, t, zc, 0);
-    if (split && g.W > 0) k_vmem<A, 1><<<sms * 8, 256, 0, st>>>(g, p, a);
-    k_gather<S, R, 1, MG><<<ggrid, block, smemg, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse);
-    if (split && a.grad && fuse) k_gather<S, R, 1, 2><<<ggrid, block, smemd, st>>>(m.v, *snapV, g, p, a, v, zc, fuse);
-    if (g.W > 0) k_vmem<A, 0><<<sms * 8, 256, 0, st>>>(g, p, a);
+    // The memory updates ride in the gradient kernels' launches when those run (their slab cells; each gradient
+    // kernel runs after the gather that reads those slots and before tmpT / tmpV is overwritten), else in k_vmem.
+    const int mt = split && a.grad && g.W > 0 && a.vmerge, mv = mt && fuse;
+    k_gather<S, R, 0, MG><<<ggrid, block, smemg, st>>>(m.t, snapT ? *snapT : m.t, g, p, a, t, zc, 0, 0);
+    if (split && a.grad) k_gather<S, R, 0, 2><<<ggrid, block, smemd, st>>>(m.t, *snapT, g, p, a, t, zc, 0, mt);
+    if (split && g.W > 0 && !mt) k_vmem<A, 1><<<sms * 8, 256, 0, st>>>(g, p, a);
+    k_gather<S, R, 1, MG><<<ggrid, block, smemg, st>>>(m.v, snapV ? *snapV : m.v, g, p, a, v, zc, fuse, 0);
+    if (split && a.grad && fuse)
+        k_gather<S, R, 1, 2><<<ggrid, block, smemd, st>>>(m.v, *snapV, g, p, a, v, zc, fuse, mv);
+    if (g.W > 0 && !mv) k_vmem<A, 0><<<sms * 8, 256, 0, st>>>(g, p, a);
     return cudaGetLastError();
 }
 
@@ -1198,7 +1245,12 @@ cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m) {
     }
     return cudaErrorInvalidValue;
 }
-bool adj_split() { return BEHF_ADJ_SPLIT != 0; }
+int adj_step_launches(const Geom& g, const AdjPtrs& a, int fuse) {
+    constexpr bool split = BEHF_ADJ_SPLIT != 0;
+    const bool mt = split && a.grad && g.W > 0 && a.vmerge, mv = mt && fuse;  // as in adj_r
+    return 2 + (split && a.grad ? 1 + (fuse ? 1 : 0) : 0) + (split && g.W > 0 && !mt ? 1 : 0) +
+           (g.W > 0 && !mv ? 1 : 0);
+}
 template <class S>
 bool adj_snap_staged() {
     return BEHF_ADJ_SPLIT || (BEHF_ADJ_SNAP && sizeof(S) == 2);

@@ -35,6 +35,7 @@ struct AdjPtrs {
     int derived;             // the forward ran the tiled kernels: VW2 = VU2 VW3 c_vw2, S3 = P1 c_s3 (the stored
                              // VW2 and S3 are not read, their gradients go to VU2, VW3 and P1)
     int pf;                  // gathers and gradient kernels: prefetch each cell's own arrays of the next plane into L2
+    int vmerge;              // the gradient kernels also do the CPML memory updates of their slab cells
 };
 
 // Tensor maps of the twelve staged arrays of one gather (x windows, y windows, z-ring rows; adjoint.cu), and of
@@ -59,8 +60,9 @@ cudaError_t adj_build_maps(const Geom& g, const AdjPtrs& a, AdjMaps* m);
 // of the step), mv over its velocities and Darcy velocities (the fused T^T of the step before).
 template <class S>
 bool adj_snap_staged();
-// The coefficient gradients run in launches of their own (two more per step) rather than inside the gathers.
-bool adj_split();
+// Kernels one adj_step launches (for the host launch count): the gathers, the gradient kernels and the memory
+// updates that do not ride in them.
+int adj_step_launches(const Geom& g, const AdjPtrs& a, int fuse);
 template <class S>
 cudaError_t adj_build_snap_maps(const Geom& g, void* const f[kNField], GatherMaps* mt, GatherMaps* mv);
 // T^T per cell of the first backward step (after its record^T).

@@ -1201,6 +1201,8 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     {  // L2 prefetch in the adjoint kernels: on unless BEHF_ADJ_PREFETCH=0 (a diagnostic switch; same results)
         const char* e = getenv("BEHF_ADJ_PREFETCH");
         a.pf = (e && e[0] == '0') ? 0 : 1;
+        const char* v = getenv("BEHF_ADJ_VMERGE");
+        a.vmerge = (v && v[0] == '0') ? 0 : 1;
     }
     // compensated summation of the FP32 accumulators: segment sums folded into running totals
     AdjFold fold{};
@@ -1480,7 +1482,7 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
                 if (fuse)
                     CK(adj_recfix<S>(g, c->p, a, c->d_rec_off, c->d_rec_comp, nrec, d_adj, nt, it - 1, sc,
                                      c->stream));
-                c->launches += 3 + (g.W > 0 ? 1 : 0) + fuse + (adj_split() ? 1 + fuse : 0);
+                c->launches += adj_step_launches(g, a, fuse) + 1 + fuse;  // + source^T, record^T
             }
             if (folding) {
                 CK(adj_fold(fold, (long long)nf, 0, c->stream));

@@ -2,7 +2,8 @@
 FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identity and finite differences):
   * FP64: wavelet and moduli gradients within 1e-9 relative L2 of the oracle, every source kind, radius 1/2/4,
     with and without CPML; dot-product identity within 1e-10; checkpoint spacing, two checkpoint levels and the
-    snapshot cache, the overlap of the recompute with the adjoint steps and the L2 prefetch change nothing;
+    snapshot cache, the overlap of the recompute with the adjoint steps, the L2 prefetch and the memory updates in
+    the gradient kernels change nothing;
   * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
   * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
 from __future__ import annotations
@@ -83,15 +84,17 @@ def test_gradient_checkpoint_spacing(behf_lib):
         np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
 
 
+@pytest.mark.parametrize("switch", ["BEHF_ADJ_PREFETCH", "BEHF_ADJ_VMERGE"])
 @pytest.mark.parametrize("precision", ["f32", "f16"])
-def test_gradient_l2_prefetch_changes_nothing(behf_lib, precision, monkeypatch):
-    # the adjoint kernels' L2 prefetch of the next plane (on by default, BEHF_ADJ_PREFETCH=0 turns it off) only
-    # moves data into L2: the same gradient, bit for bit
+def test_gradient_kernel_switches_change_nothing(behf_lib, precision, switch, monkeypatch):
+    # the adjoint kernels' L2 prefetch of the next plane only moves data into L2, and the CPML memory updates
+    # done by the gradient kernels for their slab cells are k_vmem's arithmetic: both on by default, =0 turns
+    # either off; the same gradient, bit for bit
     p = small(R=4, L=5, kind="force_z")
     adj = np.random.default_rng(11).standard_normal((len(p.rec_comp), p.nt))
-    monkeypatch.setenv("BEHF_ADJ_PREFETCH", "0")
+    monkeypatch.setenv(switch, "0")
     ref = gpu_gradient(p, adj, precision, checkpoint=13)
-    monkeypatch.setenv("BEHF_ADJ_PREFETCH", "1")
+    monkeypatch.setenv(switch, "1")
     out = gpu_gradient(p, adj, precision, checkpoint=13)
     for a, b in zip(out, ref):
         np.testing.assert_array_equal(a, b)
