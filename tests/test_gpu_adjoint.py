@@ -4,7 +4,8 @@ FP64 CPU discrete adjoint of the oracle (itself pinned by the dot-product identi
     with and without CPML; dot-product identity within 1e-10; checkpoint spacing, two checkpoint levels and the
     snapshot cache, the overlap of the recompute with the adjoint steps, the L2 prefetch and the memory updates in
     the gradient kernels change nothing;
-  * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2;
+  * FP32 storage + FP32 adjoint: within 1e-4 of the oracle; FP16 storage (FP32 adjoint): within 5e-2; BF16
+    storage within 0.35;
   * finite differences of the GPU's own FP64 misfit agree with its gradient within 1e-3."""
 from __future__ import annotations
 
@@ -121,7 +122,9 @@ def test_gradient_snapshot_cache(behf_lib, precision):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision,tol", [("f32", 1e-4), ("f16", 5e-2)])
+# measured (this problem): FP16 moduli and parameters within 2.6e-2, BF16 within 0.27 (three fewer stored
+# significand bits); the wavelet gradient (3.5e-3) does not depend on the stored forward fields
+@pytest.mark.parametrize("precision,tol", [("f32", 1e-4), ("f16", 5e-2), ("bf16", 0.35)])
 def test_gradient_reduced_precision(behf_lib, oracle, precision, tol):
     p = small(R=4, L=5, kind="explosive")
     adj = np.random.default_rng(7).standard_normal((len(p.rec_comp), p.nt))
