@@ -284,13 +284,43 @@ constexpr int GX = 32, GY = 8;
 #define BEHF_ADJ_MINB_G1 3
 #endif
 
-// The adjoint CPML memory update of one cell on every slab axis that holds it: k_vmem<A, TSLOT>'s work for that
-// cell, in a tile kernel (the gradient kernels do it for the slab cells of their tiles).  TSLOT 1: the T slots 4..7
-// from tmpT; TSLOT 0: the V slots 0..3 from tmpV.  Slot order and half-shifted profiles as in k_vmem.
+// The adjoint CPML memory update of one cell on one slab axis ax (position pos along it, slab offset so), from
+// the four derivative-group adjoints D of that axis:  lpsi = A (lpsi + D),  lprv = A B (lpsi_old + D).  TSLOT 0:
+// the V slots 0..3 from tmpV (axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x,
+// Sigma_z; z: Sigma_z, Dp_z, Sigma_x, Sigma_y); TSLOT 1: the T slots 4..7 from tmpT (axis x: uxx s4, wx s5, uyx s6h,
+// uzx s7h; y: uyy, wy, uxy, uzy; z: uzz, wz, uxz, uyz; tmpT 0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz); h: the
+// half-shifted profiles.  mem_groups gives the tmpT / tmpV index of each slot's D.
+template <int TSLOT>
+__device__ __forceinline__ void mem_groups(int ax, int (&dq)[4]) {
+    dq[0] = ax;
+    dq[1] = TSLOT ? 3 : ax + 3;
+    dq[2] = TSLOT ? (ax == 2 ? 5 : 4) : (ax == 0 ? 1 : 0);
+    dq[3] = TSLOT ? (ax == 0 ? 5 : 6) : (ax == 2 ? 1 : 2);
+}
+template <class A, int TSLOT>
+__device__ __forceinline__ void mem_axis(const DevPtrs& p, const AdjPtrs& a, int ax, int pos, long long so,
+                                         const A (&D)[4]) {
+    constexpr int SB = TSLOT ? 4 : 0;
+    A L[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) L[q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[so];
+    const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
+    const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const bool h = TSLOT ? q >= 2 : q < 2;  // half-shifted profiles: V slots 0, 1; T slots 6, 7
+        const A Ap = h ? pa2 : pa, B = h ? pb2 : pb;
+        const A Lm = L[q] + D[q];
+        reinterpret_cast<A*>(a.lpsi[ax][SB + q])[so] = Ap * Lm;
+        reinterpret_cast<A*>(a.lprv[ax][SB + q])[so] = Ap * B * Lm;
+    }
+}
+// The same update of one cell on every slab axis that holds it, in a tile kernel (the gradient kernels do it for
+// the slab cells of their tiles): k_vmem<A, TSLOT>'s work for that cell.
 template <class A, int TSLOT>
 __device__ __forceinline__ void vmem_cell(const Geom& g, const DevPtrs& p, const AdjPtrs& a, int i, int j, int k,
                                           long long c) {
-    constexpr int ND = TSLOT ? 7 : 6, SB = TSLOT ? 4 : 0;
+    constexpr int ND = TSLOT ? 7 : 6;
     A d[ND];
 #pragma unroll
     for (int q = 0; q < ND; q++) d[q] = reinterpret_cast<const A*>(TSLOT ? a.tmpT[q] : a.tmpV[q])[c];
@@ -299,22 +329,10 @@ __device__ __forceinline__ void vmem_cell(const Geom& g, const DevPtrs& p, const
         const int pos = ax == 0 ? i : ax == 1 ? j : k;
         const int s = slab_index(pos, ax == 0 ? g.nx : ax == 1 ? g.ny : g.nz, g.L);
         if (s < 0) continue;
-        const long long so = slab_off(g, ax, i, j, k, s);
-        const int dq[4] = {ax, TSLOT ? 3 : ax + 3, TSLOT ? (ax == 2 ? 5 : 4) : (ax == 0 ? 1 : 0),
-                           TSLOT ? (ax == 0 ? 5 : 6) : (ax == 2 ? 1 : 2)};
-        A L[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) L[q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[so];
-        const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
-        const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const bool h = TSLOT ? q >= 2 : q < 2;
-            const A Ap = h ? pa2 : pa, B = h ? pb2 : pb;
-            const A Lm = L[q] + d[dq[q]];
-            reinterpret_cast<A*>(a.lpsi[ax][SB + q])[so] = Ap * Lm;
-            reinterpret_cast<A*>(a.lprv[ax][SB + q])[so] = Ap * B * Lm;
-        }
+        int dq[4];
+        mem_groups<TSLOT>(ax, dq);
+        const A D[4] = {d[dq[0]], d[dq[1]], d[dq[2]], d[dq[3]]};
+        mem_axis<A, TSLOT>(p, a, ax, pos, slab_off(g, ax, i, j, k, s), D);
     }
 }
 
@@ -944,28 +962,12 @@ __global__ void k_vmem(Geom g, DevPtrs p, AdjPtrs a) {
         }
         if (i < g.R || i >= g.nx - g.R || j < g.R || j >= g.ny - g.R || k < g.R || k >= g.nz - g.R) continue;
         const long long c = (long long)k * g.plane + (long long)j * g.px + i;
-        // V slots, axis x: Sigma_x s0h, Dp_x s1h, Sigma_y s2, Sigma_z s3; y: Sigma_y, Dp_y, Sigma_x, Sigma_z;
-        // z: Sigma_z, Dp_z, Sigma_x, Sigma_y.  T slots, axis x: uxx s4, wx s5, uyx s6h, uzx s7h; y: uyy, wy,
-        // uxy, uzy; z: uzz, wz, uxz, uyz (tmpT 0 uxx, 1 uyy, 2 uzz, 3 w, 4 xy, 5 xz, 6 yz)
-        const int dq[4] = {ax, TSLOT ? 3 : ax + 3, TSLOT ? (ax == 2 ? 5 : 4) : (ax == 0 ? 1 : 0),
-                           TSLOT ? (ax == 0 ? 5 : 6) : (ax == 2 ? 1 : 2)};
-        constexpr int SB = TSLOT ? 4 : 0;
-        A D[4], L[4];
+        int dq[4];
+        mem_groups<TSLOT>(ax, dq);
+        A D[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            D[q] = reinterpret_cast<const A*>(TSLOT ? a.tmpT[dq[q]] : a.tmpV[dq[q]])[c];
-            L[q] = reinterpret_cast<const A*>(a.lpsi[ax][SB + q])[u];
-        }
-        const A pa = reinterpret_cast<const A*>(p.pa[ax])[pos], pb = reinterpret_cast<const A*>(p.pb[ax])[pos];
-        const A pa2 = reinterpret_cast<const A*>(p.pa2[ax])[pos], pb2 = reinterpret_cast<const A*>(p.pb2[ax])[pos];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const bool h = TSLOT ? q >= 2 : q < 2;  // half-shifted profiles: V slots 0, 1; T slots 6, 7
-            const A Ap = h ? pa2 : pa, B = h ? pb2 : pb;
-            const A Lm = L[q] + D[q];
-            reinterpret_cast<A*>(a.lpsi[ax][SB + q])[u] = Ap * Lm;
-            reinterpret_cast<A*>(a.lprv[ax][SB + q])[u] = Ap * B * Lm;
-        }
+        for (int q = 0; q < 4; q++) D[q] = reinterpret_cast<const A*>(TSLOT ? a.tmpT[dq[q]] : a.tmpV[dq[q]])[c];
+        mem_axis<A, TSLOT>(p, a, ax, pos, u, D);
     }
 }
 
