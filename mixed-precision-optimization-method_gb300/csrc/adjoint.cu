@@ -569,6 +569,16 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
                 Q::template pf<K>(p.k[VW3X + d], cn);
                 if (!a.derived) Q::template pf<K>(p.k[VW2X + d], cn);
             }
+            if (MODE == 0 && a.grad && inn) {  // the fused V-coefficient gradients
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    Q::template pf<S>(a.qprev[d], cn);
+                    Q::template pf<S>(a.cur[BEHF_QX + d], cn);
+                }
+#pragma unroll
+                for (int q = 0; q < 15; q++)
+                    if (!(a.derived && q >= VW2X && q <= VW2Z)) Q::template pf<A>(a.g[q], cn);
+            }
         } else {
 #pragma unroll
             for (int q = 0; q < 7; q++) Q::template pf<A>(a.lf[BEHF_SXX + q], cn);
@@ -576,6 +586,10 @@ __global__ void __launch_bounds__(256, MODE == 0 ? BEHF_ADJ_MINB
 #pragma unroll
                 for (int q = 0; q < 8; q++)
                     if (q != 4 || !a.derived) Q::template pf<K>(p.k[P1 + q], cn);
+            if (MODE == 0 && fuse && a.grad && inn)  // the fused T-coefficient gradients
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    if (q != 4 || !a.derived) Q::template pf<A>(a.g[P1 + q], cn);
         }
     };
     bool failed = false;
