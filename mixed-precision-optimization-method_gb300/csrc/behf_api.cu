@@ -1198,7 +1198,8 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     CK(cudaMemsetAsync(d_gfac, 0, 8, c->stream));
     a.grad = 1;
     a.derived = (c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok) ? 1 : 0;
-    {  // L2 prefetch in the adjoint kernels: on unless BEHF_ADJ_PREFETCH=0 (a diagnostic switch; same results)
+    {  // the adjoint kernels' L2 prefetch and the memory updates inside the gradient kernels: on unless
+       // BEHF_ADJ_PREFETCH=0 / BEHF_ADJ_VMERGE=0 (diagnostic switches for timing; the same results)
         const char* e = getenv("BEHF_ADJ_PREFETCH");
         a.pf = (e && e[0] == '0') ? 0 : 1;
         const char* v = getenv("BEHF_ADJ_VMERGE");
