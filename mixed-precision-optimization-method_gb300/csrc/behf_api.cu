@@ -1324,7 +1324,9 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
     const long long so = c->cell_offset(c->src_ijk[0], c->src_ijk[1], c->src_ijk[2]);
     // one forward step with the d_it counter, keeping the fields after V (+ force) in slot idx of segment sg
     // (idx < 0: no snapshot)
-    auto snap_step = [&](int sg, int idx, bool record) -> cudaError_t {
+    // (to_snapshot: stop after the snapshot, without the stress update and the tick; the out-of-place recompute
+    // below does those for the step with its next step)
+    auto snap_step = [&](int sg, int idx, bool record, bool to_snapshot = false) -> cudaError_t {
         cudaError_t e;
         if (c->src_kind != BEHF_SRC_FORCE_Z &&
             (e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
@@ -1334,6 +1336,10 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
             (e = aux_source<S>(c->p, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
             return e;
         if (idx >= 0 && (e = snap_fields(sg, idx)) != cudaSuccess) return e;
+        if (to_snapshot) {
+            c->launches += 2;
+            return cudaSuccess;
+        }
         if ((e = dispatch_update(c, false)) != cudaSuccess) return e;
         if (record) {
             RecScales rs;
@@ -1346,6 +1352,31 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
         return aux_tick(c->d_it, 1, c->stream);
     };
 
+    // The recompute steps out of place with the kernels that read the fields only through tensor maps (the
+    // warp-specialised and tensor-memory variants; the classic and plain kernels read them directly): instead of
+    // copying 13 fields into each snapshot slot, the stress update of step it - 1 reads slot u - 1 and writes the
+    // stresses and pressure of slot u, and the velocity update of step it reads slot u - 1's velocities and slot
+    // u's stresses and writes slot u's velocities.  The CPML memory stays in place, updated in the same order.
+    // BEHF_RC_OOP=0 keeps the copies (a diagnostic switch; the same results).
+    const char* oop_env = getenv("BEHF_RC_OOP");
+    const bool oop = !(oop_env && oop_env[0] == '0') && c->kernel_opt != BEHF_KERNEL_PLAIN && c->tiled_ok &&
+                     c->g.ws >= 1 && sizeof(S) < 8;
+    std::unique_ptr<void, decltype(&std::free)> ovm(nullptr, &std::free), otm(nullptr, &std::free);
+    if (oop) {  // the field maps are re-encoded per step; the rest are the context's
+        ovm.reset(std::aligned_alloc(64, (sizeof(tiled::VMaps) + 63) / 64 * 64));
+        otm.reset(std::aligned_alloc(64, (sizeof(tiled::TMaps) + 63) / 64 * 64));
+        if (!ovm || !otm) return fail(BEHF_ERR_ALLOC, "out of host memory");
+        std::memcpy(ovm.get(), c->vmaps, sizeof(tiled::VMaps));
+        std::memcpy(otm.get(), c->tmaps, sizeof(tiled::TMaps));
+        // the updates write only the updated cells: the slots' ghost ring must hold the zeros a copy of the
+        // fields would bring (ordered before the backward pass by the synchronisation after the forward pass)
+        CK(cudaMemsetAsync(snap, 0, snap_bytes * (S_ + 1), c->stream));
+        if (snap2) CK(cudaMemsetAsync(snap2, 0, snap_bytes * (S_ + 1), c->stream));
+    }
+    auto launch_maps = [&](const DevPtrs& po, const void* maps, bool vel) -> cudaError_t {
+        return c->tile_rows == 4 ? launch_tiled_rows4<S>(c->g, po, maps, vel, c->stream)
+                                 : launch_tiled<S>(c->g, po, maps, vel, c->stream);
+    };
     // recompute a segment from its checkpoint on c->stream, keeping the fields after V (+ force) of every step
     auto recompute = [&](int sg, int s0, int s1, char* ckp) -> cudaError_t {
         cudaError_t e;
@@ -1353,8 +1384,35 @@ behf_status gradient_impl(behf_ctx* c, int nt, const double* adj_host, const dou
         if ((e = cudaMemsetAsync(c->d_it, 0, sizeof(int), c->stream)) != cudaSuccess) return e;
         if (s0 > 0 && (e = aux_tick(c->d_it, s0, c->stream)) != cudaSuccess) return e;
         if ((e = snap_fields(sg, 0)) != cudaSuccess) return e;
-        for (int it = s0; it < s1; it++)
-            if ((e = snap_step(sg, it - s0 + 1, false)) != cudaSuccess) return e;
+        if (!oop) {
+            for (int it = s0; it < s1; it++)
+                if ((e = snap_step(sg, it - s0 + 1, false)) != cudaSuccess) return e;
+            return cudaSuccess;
+        }
+        // step s0 in place up to its snapshot (slot 1); the segment's last stress update is not needed
+        if ((e = snap_step(sg, 1, false, true)) != cudaSuccess) return e;
+        for (int u = 2; u <= s1 - s0; u++) {
+            void *prev[kNField], *vf[kNField];
+            DevPtrs po = c->p;
+            for (int q = 0; q < kNField; q++) {
+                prev[q] = snap_ptr(sg, u - 1, q);
+                po.f[q] = snap_ptr(sg, u, q);
+                vf[q] = q <= BEHF_QZ ? prev[q] : po.f[q];
+            }
+            e = c->tile_rows == 4 ? tiled_field_maps_rows4<S>(c->g, vf, prev, ovm.get(), otm.get())
+                                  : tiled_field_maps<S>(c->g, vf, prev, ovm.get(), otm.get());
+            if (e != cudaSuccess) return e;
+            if ((e = launch_maps(po, otm.get(), false)) != cudaSuccess) return e;  // stresses of step it - 1
+            if ((e = aux_tick(c->d_it, 1, c->stream)) != cudaSuccess) return e;
+            if (c->src_kind != BEHF_SRC_FORCE_Z &&
+                (e = aux_source<S>(po, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
+                return e;
+            if ((e = launch_maps(po, ovm.get(), true)) != cudaSuccess) return e;  // velocities of step it
+            if (c->src_kind == BEHF_SRC_FORCE_Z &&
+                (e = aux_source<S>(po, so, c->src_kind, c->d_wavelet, c->nw, c->d_it, 0, fac, c->stream)) != cudaSuccess)
+                return e;
+            c->launches += 4;
+        }
         return cudaSuccess;
     };
     // the second stream of the overlap and its events (done: a buffer's recompute finished; free: the adjoint

@@ -220,9 +220,13 @@ template <class S> cudaError_t launch_plain(const Geom& g, const DevPtrs& p, boo
 template <class S> cudaError_t launch_tiled(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st);
 template <class S> bool tiled_supported(const Geom& g);
 template <class S> cudaError_t tiled_build_maps(const Geom& g, const DevPtrs& p, void* vmaps, void* tmaps);
+// Re-encode only the field maps of built maps: vf the 13 arrays the velocity kernel reads, tf the stress kernel's.
+template <class S> cudaError_t tiled_field_maps(const Geom& g, void* const* vf, void* const* tf, void* vmaps, void* tmaps);
 // The same with 4-row tiles (kernels_tiled_<type>_rows4.cu).
 template <class S> cudaError_t launch_tiled_rows4(const Geom& g, const DevPtrs& p, const void* maps, bool vel, cudaStream_t st);
 template <class S> bool tiled_supported_rows4(const Geom& g);
 template <class S> cudaError_t tiled_build_maps_rows4(const Geom& g, const DevPtrs& p, void* vmaps, void* tmaps);
+template <class S> cudaError_t tiled_field_maps_rows4(const Geom& g, void* const* vf, void* const* tf, void* vmaps,
+                                                      void* tmaps);
 
 }  // namespace behf

@@ -11,6 +11,14 @@ cudaError_t tiled_build_maps<double>(const Geom&, const DevPtrs&, void*, void*) 
     return cudaErrorNotSupported;
 }
 template <>
+cudaError_t tiled_field_maps<double>(const Geom&, void* const*, void* const*, void*, void*) {
+    return cudaErrorNotSupported;
+}
+template <>
+cudaError_t tiled_field_maps_rows4<double>(const Geom&, void* const*, void* const*, void*, void*) {
+    return cudaErrorNotSupported;
+}
+template <>
 cudaError_t launch_tiled<double>(const Geom&, const DevPtrs&, const void*, bool, cudaStream_t) {
     return cudaErrorNotSupported;
 }

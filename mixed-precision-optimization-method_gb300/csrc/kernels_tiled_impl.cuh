@@ -695,46 +695,56 @@ namespace behf {
 namespace BEHF_TILED_NAMESPACE {
 
 // ----------------------------------------------------------------------------------------- host side
+// The field tensor maps: vf the arrays the velocity kernel reads (stresses and pressure in halo and z-lead boxes,
+// its own velocities and Darcy velocities), tf the arrays the stress kernel reads.  Both are the context's fields
+// for an in-place step; the gradient's recompute passes snapshot slots instead and steps out of place (the
+// warp-specialised and tensor-memory kernels read fields only through these maps and store through DevPtrs::f).
 template <class S, int R>
-bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
+bool field_maps_r(const Geom& g, void* const* vf, void* const* tf, VMaps* vm, TMaps* tm) {
     typedef Geo<S, R> G;
     bool ok = true;
     // velocity
-    ok &= encode<S>(&vm->halo[0], g, p.f[BEHF_SXX], G::BW, TY);
-    ok &= encode<S>(&vm->halo[1], g, p.f[BEHF_SYY], TXC, G::BH);
-    ok &= encode<S>(&vm->halo[2], g, p.f[BEHF_SXY], G::BW, G::BH);
-    ok &= encode<S>(&vm->halo[3], g, p.f[BEHF_SXZ], G::BW, TY);
-    ok &= encode<S>(&vm->halo[4], g, p.f[BEHF_SYZ], TXC, G::BH);
-    ok &= encode<S>(&vm->halo[5], g, p.f[BEHF_P], G::BW, G::BH);
-    ok &= encode<S>(&vm->zlead[0], g, p.f[BEHF_SZZ], TXC, TY);
-    ok &= encode<S>(&vm->zlead[1], g, p.f[BEHF_SXZ], TXC, TY);
-    ok &= encode<S>(&vm->zlead[2], g, p.f[BEHF_SYZ], TXC, TY);
-    ok &= encode<S>(&vm->zlead[3], g, p.f[BEHF_P], TXC, TY);
+    ok &= encode<S>(&vm->halo[0], g, vf[BEHF_SXX], G::BW, TY);
+    ok &= encode<S>(&vm->halo[1], g, vf[BEHF_SYY], TXC, G::BH);
+    ok &= encode<S>(&vm->halo[2], g, vf[BEHF_SXY], G::BW, G::BH);
+    ok &= encode<S>(&vm->halo[3], g, vf[BEHF_SXZ], G::BW, TY);
+    ok &= encode<S>(&vm->halo[4], g, vf[BEHF_SYZ], TXC, G::BH);
+    ok &= encode<S>(&vm->halo[5], g, vf[BEHF_P], G::BW, G::BH);
+    ok &= encode<S>(&vm->zlead[0], g, vf[BEHF_SZZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[1], g, vf[BEHF_SXZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[2], g, vf[BEHF_SYZ], TXC, TY);
+    ok &= encode<S>(&vm->zlead[3], g, vf[BEHF_P], TXC, TY);
+    for (int a = 0; a < 3; a++) {
+        ok &= encode<S>(&vm->own[a], g, vf[BEHF_VX + a], TXC, TY);
+        ok &= encode<S>(&vm->own[3 + a], g, vf[BEHF_QX + a], TXC, TY);
+    }
     // stress
-    ok &= encode<S>(&tm->halo[0], g, p.f[BEHF_VX], G::BW, G::BH);
-    ok &= encode<S>(&tm->halo[1], g, p.f[BEHF_VY], G::BW, G::BH);
-    ok &= encode<S>(&tm->halo[2], g, p.f[BEHF_VZ], G::BW, G::BH);
-    ok &= encode<S>(&tm->halo[3], g, p.f[BEHF_QX], G::BW, TY);
-    ok &= encode<S>(&tm->halo[4], g, p.f[BEHF_QY], TXC, G::BH);
-    ok &= encode<S>(&tm->zlead[0], g, p.f[BEHF_VX], TXC, TY);
-    ok &= encode<S>(&tm->zlead[1], g, p.f[BEHF_VY], TXC, TY);
-    ok &= encode<S>(&tm->zlead[2], g, p.f[BEHF_VZ], TXC, TY);
-    ok &= encode<S>(&tm->zlead[3], g, p.f[BEHF_QZ], TXC, TY);
+    ok &= encode<S>(&tm->halo[0], g, tf[BEHF_VX], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[1], g, tf[BEHF_VY], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[2], g, tf[BEHF_VZ], G::BW, G::BH);
+    ok &= encode<S>(&tm->halo[3], g, tf[BEHF_QX], G::BW, TY);
+    ok &= encode<S>(&tm->halo[4], g, tf[BEHF_QY], TXC, G::BH);
+    ok &= encode<S>(&tm->zlead[0], g, tf[BEHF_VX], TXC, TY);
+    ok &= encode<S>(&tm->zlead[1], g, tf[BEHF_VY], TXC, TY);
+    ok &= encode<S>(&tm->zlead[2], g, tf[BEHF_VZ], TXC, TY);
+    ok &= encode<S>(&tm->zlead[3], g, tf[BEHF_QZ], TXC, TY);
+    for (int q = 0; q < 7; q++) ok &= encode<S>(&tm->own[q], g, tf[BEHF_SXX + q], TXC, TY);
+    return ok;
+}
+
+template <class S, int R>
+bool build_maps_r(const Geom& g, const DevPtrs& p, VMaps* vm, TMaps* tm) {
+    bool ok = field_maps_r<S, R>(g, p.f, p.f, vm, tm);
     // own-cell boxes (warp-specialised kernels)
     typedef typename Traits<S>::K K;
     typedef typename Traits<S>::W Wt;
     for (int a = 0; a < 3; a++) {
-        ok &= encode<S>(&vm->own[a], g, p.f[BEHF_VX + a], TXC, TY);
-        ok &= encode<S>(&vm->own[3 + a], g, p.f[BEHF_QX + a], TXC, TY);
         ok &= encode<Wt>(&vm->own[6 + a], g, p.k[VW1X + a], TXC, TY);
         ok &= encode<K>(&vm->own[9 + a], g, p.k[VW3X + a], TXC, TY);
         ok &= encode<K>(&vm->own[12 + a], g, p.k[VU1X + a], TXC, TY);
         ok &= encode<K>(&vm->own[15 + a], g, p.k[VU2X + a], TXC, TY);
     }
-    for (int q = 0; q < 7; q++) {
-        ok &= encode<S>(&tm->own[q], g, p.f[BEHF_SXX + q], TXC, TY);
-        ok &= encode<K>(&tm->own[7 + q], g, p.k[q < 4 ? P1 + q : P1 + q + 1], TXC, TY);
-    }
+    for (int q = 0; q < 7; q++) ok &= encode<K>(&tm->own[7 + q], g, p.k[q < 4 ? P1 + q : P1 + q + 1], TXC, TY);
     // x-slab CPML memory and x profiles, staged by the tensor-memory kernels (FP32 memory)
     if (g.W > 0 && g.xs_bw > 0 && sizeof(Wt) == 4) {
         for (int j = 0; j < 4; j++) {
@@ -856,6 +866,20 @@ cudaError_t launch_r(const Geom& g, const DevPtrs& p, const void* maps, bool vel
             case 2: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 2>(g, p, v, t); break;                                      \
             case 3: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 3>(g, p, v, t); break;                                      \
             case 4: ok = BEHF_TILED_NAMESPACE::build_maps_r<S, 4>(g, p, v, t); break;                                      \
+        }                                                                                                  \
+        return ok ? cudaSuccess : cudaErrorInvalidValue;                                                   \
+    }                                                                                                      \
+    template <>                                                                                            \
+    cudaError_t BEHF_TILED_FN(tiled_field_maps)<S>(const Geom& g, void* const* vf, void* const* tf, void* vm,    \
+                                                   void* tm) {                                             \
+        bool ok = false;                                                                                   \
+        auto* v = reinterpret_cast<BEHF_TILED_NAMESPACE::VMaps*>(vm);                                      \
+        auto* t = reinterpret_cast<BEHF_TILED_NAMESPACE::TMaps*>(tm);                                      \
+        switch (g.R) {                                                                                     \
+            case 1: ok = BEHF_TILED_NAMESPACE::field_maps_r<S, 1>(g, vf, tf, v, t); break;                 \
+            case 2: ok = BEHF_TILED_NAMESPACE::field_maps_r<S, 2>(g, vf, tf, v, t); break;                 \
+            case 3: ok = BEHF_TILED_NAMESPACE::field_maps_r<S, 3>(g, vf, tf, v, t); break;                 \
+            case 4: ok = BEHF_TILED_NAMESPACE::field_maps_r<S, 4>(g, vf, tf, v, t); break;                 \
         }                                                                                                  \
         return ok ? cudaSuccess : cudaErrorInvalidValue;                                                   \
     }                                                                                                      \

@@ -85,12 +85,12 @@ def test_gradient_checkpoint_spacing(behf_lib):
         np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
 
 
-@pytest.mark.parametrize("switch", ["BEHF_ADJ_PREFETCH", "BEHF_ADJ_VMERGE"])
+@pytest.mark.parametrize("switch", ["BEHF_ADJ_PREFETCH", "BEHF_ADJ_VMERGE", "BEHF_RC_OOP"])
 @pytest.mark.parametrize("precision", ["f32", "f16"])
 def test_gradient_kernel_switches_change_nothing(behf_lib, precision, switch, monkeypatch):
-    # the adjoint kernels' L2 prefetch of the next plane only moves data into L2, and the CPML memory updates
-    # done by the gradient kernels for their slab cells are k_vmem's arithmetic: both on by default, =0 turns
-    # either off; the same gradient, bit for bit
+    # the adjoint kernels' L2 prefetch of the next plane only moves data into L2, the CPML memory updates done
+    # by the gradient kernels for their slab cells are k_vmem's arithmetic, and the out-of-place recompute writes
+    # the snapshot slots the copies would fill: all on by default, =0 turns one off; the same gradient, bit for bit
     p = small(R=4, L=5, kind="force_z")
     adj = np.random.default_rng(11).standard_normal((len(p.rec_comp), p.nt))
     monkeypatch.setenv(switch, "0")
@@ -101,7 +101,7 @@ def test_gradient_kernel_switches_change_nothing(behf_lib, precision, switch, mo
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision", ["f64", "f16"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16"])
 def test_gradient_snapshot_cache(behf_lib, precision):
     # every segment recomputed (0), the last two kept from the forward pass (50 MiB of 1.6 MB slots x 13 per
     # segment at f64), all kept (-1): the same gradient, bit for bit; and the recomputes overlapped with the
